@@ -1,0 +1,27 @@
+#!/usr/bin/env bash
+# Build oracle/_ref/libvpmc_ref.so from the reference's own CPU sources, read
+# in place from the reference tree (default /root/reference, override with
+# VPMC_REFERENCE_DIR), plus oracle/ref_shim.cpp.  Test infrastructure only:
+# the output is git-ignored and used to pin the oracle and make golden
+# vectors.  Exits 0 without building when the reference tree is absent.
+set -euo pipefail
+here="$(cd "$(dirname "$0")" && pwd)"
+ref="${VPMC_REFERENCE_DIR:-/root/reference}"
+out="$here/_ref"
+if [ ! -d "$ref/src/cpu" ]; then
+    echo "build_ref: reference tree not found at $ref; skipping" >&2
+    exit 0
+fi
+mkdir -p "$out/stub/thrust"
+# src/utilities.cu includes <thrust/host_vector.h> unconditionally although its
+# CPU branch does not use it; an empty stub lets it compile as C++.
+: > "$out/stub/thrust/host_vector.h"
+CXX="${CXX:-g++}"
+flags=(-std=c++20 -O2 -fPIC -fopenmp -ffp-contract=off -w
+       -I"$ref/include" -I"$out/stub")
+srcs=("$ref/src/cpu/hash.cpp" "$ref/src/omp/hash_omp.cpp"
+      "$ref/src/cpu/evaluate_vorticity.cpp" "$ref/src/cpu/monte_carlo_bs.cpp"
+      "$ref/src/cpu/monte_carlo_sampling.cpp" "$ref/src/cpu/build_particle_sets.cpp")
+"$CXX" "${flags[@]}" -shared -o "$out/libvpmc_ref.so" \
+    "$here/ref_shim.cpp" "${srcs[@]}" -x c++ "$ref/src/utilities.cu" -x none
+echo "build_ref: wrote $out/libvpmc_ref.so"
