@@ -1,0 +1,262 @@
+/*
+ * vpmc.h -- C ABI of the GB300 (sm_103a) vortex-particle Monte-Carlo hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns a
+ * vpmc_status (0 = success) and never aborts.  Device pointers are CUDA
+ * global-memory addresses on the context's device; entry points whose name
+ * ends in `_host` take host pointers and do the copies themselves.  Work is
+ * issued on the context's stream; a call returns when its results are
+ * complete unless documented otherwise.  A context (and every handle made
+ * from it) must not be used by two host threads at once.
+ *
+ * The comment on each entry point cites the reference interface it replaces
+ * (file:line inside the reference project GargantuaOmni/VortexParticleMC_cuda).
+ * Layouts follow the reference: positions are float2 (x,y interleaved), the
+ * deformation F is float4 {a,b,c,d} (row-major 2x2), strengths are float.
+ */
+#ifndef VPMC_H
+#define VPMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VPMC_ABI_VERSION 1
+
+typedef enum vpmc_status {
+    VPMC_OK = 0,
+    VPMC_ERR_INVALID = 1,        /* bad argument (NULL, negative size, ...)        */
+    VPMC_ERR_UNSUPPORTED = 2,    /* backend/feature not provided (CPU/OMP paths)   */
+    VPMC_ERR_CUDA = 3,           /* a CUDA runtime call failed                     */
+    VPMC_ERR_NOMEM = 4,          /* device allocation failed                       */
+    VPMC_ERR_TIMEOUT = 5,        /* a bounded device wait expired                  */
+    VPMC_ERR_DEVICE = 6,         /* a kernel reported an internal error            */
+    VPMC_ERR_GEOMETRY = 7,       /* domain/grid too small for the neighbour walk   */
+    VPMC_ERR_CAPACITY = 8,       /* a size exceeds a documented maximum            */
+    VPMC_ERR_NOT_CONVERGED = 9,  /* iterative solve stopped before its tolerance   */
+    VPMC_ERR_NONFINITE = 10      /* NaN/Inf found in an input or a result          */
+} vpmc_status;
+
+typedef struct vpmc_context vpmc_context;
+typedef struct vpmc_sim vpmc_sim;
+
+/* Estimator law for the MIS Biot-Savart velocity.
+ *   VPMC_LAW_REFERENCE reproduces the sampling law of
+ *     monte_carlo_bs_kernel_safe (src/cuda/monte_carlo_bs.cu:144-271):
+ *     branch-1 jitter radius = iCDF table * h_w (the table already holds h_w),
+ *     disk radius R*sqrt(u) weighted as alpha/r, minimum-image r in alpha/r,
+ *     periodic field query.  Biased (its mean is not the Biot-Savart integral),
+ *     kept for variance parity and like-for-like speed.
+ *   VPMC_LAW_UNBIASED draws the branch-1 jitter from the cubic spline itself,
+ *     the disk radius uniformly in r (density alpha/r), uses raw distances
+ *     and restricts the field to the 3x3 periodic images the branch-1 density
+ *     covers, so its mean is the velocity of the smoothed field. */
+typedef enum vpmc_law { VPMC_LAW_REFERENCE = 0, VPMC_LAW_UNBIASED = 1 } vpmc_law;
+
+/* Direct-sum kernels. */
+typedef enum vpmc_direct_kernel {
+    VPMC_DIRECT_MOLLIFIED = 0,  /* smoothed-field velocity, 3x3 periodic images (oracle of the MC mean) */
+    VPMC_DIRECT_PLUMMER = 1     /* biot_savart_naive_kernel: Plummer core, minimum image, j != i        */
+} vpmc_direct_kernel;
+
+/* ------------------------------------------------------------------ context */
+/* Create a context on `device`.  `stream` may be NULL (the context creates a
+ * non-blocking stream) or a cudaStream_t the caller owns.  No reference
+ * counterpart: the reference runs everything on the default stream. */
+int vpmc_context_create(int device, void* stream, vpmc_context** out);
+int vpmc_context_destroy(vpmc_context* ctx);
+/* Stream the context issues work on (a cudaStream_t). */
+void* vpmc_context_stream(vpmc_context* ctx);
+/* Wait for all work issued on the context; returns the first pending error. */
+int vpmc_context_sync(vpmc_context* ctx);
+/* Bytes of device scratch the context currently holds. */
+size_t vpmc_context_scratch_bytes(vpmc_context* ctx);
+const char* vpmc_status_string(int status);
+int vpmc_abi_version(void);
+/* Number of kernels this library has launched in this process (all contexts):
+ * a counter for benchmarks that report GPU launch counts. */
+uint64_t vpmc_kernel_launch_count(void);
+
+/* --------------------------------------------------------------- hash (a1-a3)
+ * Uniform-grid spatial hash of a particle subset, bit-exact with the
+ * reference's deterministic CPU build (cells ascending, members ascending by
+ * local index within a cell). */
+
+/* FillCells_cuda, src/cuda/hash.cu:42-69 (and FillCells_cpu, src/cpu/hash.cpp:
+ * 6-34).  For i < N: j = sub[i]; cell = clamp(floor(x*rshx/Lx)) * rshy +
+ * clamp(floor(y*rshy/Ly)); vp_cell[i] = cell; cell_num = per-cell counts;
+ * cell_acc = exclusive prefix of cell_num.  All pointers are device pointers;
+ * cell_num/cell_acc hold rshx*rshy ints. */
+int vpmc_fill_cells(vpmc_context* ctx, int rshx, int rshy, float Lx, float Ly, int N,
+                    const int* sub, const float* pos, int* cell_num, int* cell_acc,
+                    int* vp_cell);
+
+/* CountingSort_cuda, src/cuda/hash.cu:71-91 (CountingSort_cpu, src/cpu/hash.cpp:
+ * 36-48).  vp_sort[cell_acc[c] + k] = k-th local index (ascending) of cell c;
+ * cell_num is left all-zero as the reference leaves it.  `ncell` = number of
+ * cells (the reference infers it); pass <= 0 to have it computed (one extra
+ * device-to-host read).  Deterministic, unlike the reference's atomicSub
+ * scatter. */
+int vpmc_counting_sort(vpmc_context* ctx, int N, int ncell, int* cell_num,
+                       const int* cell_acc, const int* vp_cell, int* vp_sort);
+
+/* FillCells + CountingSort in one call (the pair Simulation::do_spatial_hashing
+ * issues per subset, src/vortex_particle_mc.cu:140-164).  cell_num may be NULL. */
+int vpmc_hash_build(vpmc_context* ctx, int rshx, int rshy, float Lx, float Ly, int N,
+                    const int* sub, const float* pos, int* cell_num, int* cell_acc,
+                    int* vp_cell, int* vp_sort);
+
+/* Same as vpmc_hash_build with host buffers (copies in and out). */
+int vpmc_hash_build_host(vpmc_context* ctx, int rshx, int rshy, float Lx, float Ly, int N,
+                         int n_pos, const int* sub, const float* pos, int* cell_num,
+                         int* cell_acc, int* vp_cell, int* vp_sort);
+
+/* --------------------------------------------------------------- subsets (a4)
+ * build_subsets_cuda, src/cuda/build_particle_sets.cu:11-89: split particle
+ * indices by the sign of omega (zeros belong to neither), |omega| prefix sums
+ * normalised to a CDF, and the totals.  The CDF and totals are FP64 (the
+ * reference is FP32).  cdf32_* (optional, may be NULL) receive the FP32 copy
+ * the reference's layout uses.  cnt[2] and cum[2] are HOST pointers. */
+int vpmc_build_subsets(vpmc_context* ctx, int N, const float* omega, int* sub_pos,
+                       int* sub_neg, double* cdf_pos, double* cdf_neg, float* cdf32_pos,
+                       float* cdf32_neg, int* cnt, double* cum);
+
+/* --------------------------------------------------------- kernel table (a5)
+ * build_cubic_rcdf + cdf_to_icdf, src/utilities.cu:12-96 (host arithmetic, same
+ * FP32 steps).  Writes `length` floats each to HOST arrays (icdf may be NULL). */
+int vpmc_kernel_icdf_table(float h_w, int length, float* cdf, float* icdf);
+
+/* Cubic B-spline W(r; h_w), include/utilities.hpp:7-17, host evaluation. */
+float vpmc_cubic_spline(float r, float h_w);
+
+/* ------------------------------------------------------ vorticity query (a7)
+ * queryVorticityAbs, include/vorticity_query.cuh:15-79, for M points at once:
+ *   out[m] = sum_i  wv_i * W(|F_i^-1 d_i|; h_w),  d_i = x_i - p_m (nearest
+ *   periodic image when periodic), over particles with omega_i > 0 (sign > 0),
+ *   omega_i < 0 (sign < 0) or all (sign == 0); wv_i = omega_i if use_signed
+ *   else |omega_i|; exclude_center drops pairs closer than 1e-6.
+ * F may be NULL (identity).  Points are wrapped into the domain when periodic
+ * and give 0 outside it otherwise.  Each particle contributes once, also when
+ * the reference's hash would have fewer than 3 cells per axis (where its
+ * 3x3 walk visits cells twice).  pos/omega/F/pts/out are device pointers. */
+int vpmc_query_vorticity(vpmc_context* ctx, int N, const float* pos, const float* omega,
+                         const float* F, int M, const float* pts, int sign,
+                         int use_signed, int exclude_center, float h_w, float Lx,
+                         float Ly, int periodic, float* out);
+
+/* ---------------------------------------------------------- RBF / CG (a10)
+ * Ax_cuda, src/cuda/cg_rbf_init.cu:33-50 (matvec_kernel :11-31):
+ *   y_i = sum_j x_j W(|x_j - x_i|; h_w) over all particles (nearest image).
+ * `precise` != 0 evaluates and accumulates in-support pairs in FP64; 0 uses
+ * FP32 pair arithmetic with compensated FP32 sums.  Device pointers. */
+int vpmc_rbf_matvec(vpmc_context* ctx, int N, const float* pos, const float* x, float* y,
+                    float h_w, float Lx, float Ly, int periodic, int precise);
+
+/* conjugate_gradient_rbf, src/cuda/cg_rbf_init.cu:53-116: solve A w = b with
+ * A as above, w0 = b / W(0), stop when |r|/|b| < tol or after max_iter
+ * iterations.  Dot products and norms are FP64.  omega_out (device) receives
+ * w.  info (HOST, may be NULL) receives {iterations, recursive |r|/|b|,
+ * true |b - A w|/|b| recomputed with the FP64 SpMV}.  Returns
+ * VPMC_ERR_NOT_CONVERGED (with omega_out written) when max_iter is reached. */
+int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b,
+                float* omega_out, float h_w, float Lx, float Ly, int periodic,
+                double tol, int max_iter, double* info);
+
+/* ------------------------------------------------------ direct sums (a11)
+ * biot_savart_naive_kernel, src/cuda/naive_biot_savart.cu:15-40, in FP64.
+ * VPMC_DIRECT_PLUMMER: targets are particle indices `tidx` (M of them),
+ *   u_i = sum_{j != i} omega_j perp(d)/(2 pi (|d|^2 + eps^2)), d minimum image.
+ * VPMC_DIRECT_MOLLIFIED: targets are points `pts` (M of them), velocity of the
+ *   smoothed field over the 3x3 periodic images (or the domain alone when
+ *   !periodic): sum omega_j perp(d)/(2 pi |d|^2) M(|d|/h_w), M the spline mass.
+ * out_uv: 2*M doubles (device).  param = eps (Plummer) or h_w (mollified). */
+int vpmc_direct_velocity_f64(vpmc_context* ctx, int kernel, int N, const float* pos,
+                             const float* omega, int M, const float* pts, const int* tidx,
+                             double param, double Lx, double Ly, int periodic,
+                             double* out_uv);
+
+/* ------------------------------------------------- simulation (a8, a9, a12)
+ * SimParam, include/vortex_particle_mc.hpp:96-134; one entry per instance.
+ * h = Lx/Nx, h_w = h*hwr, dx = h_w/2 are derived as the reference does.  */
+typedef struct vpmc_sim_params {
+    float    dt;
+    float    Lx, Ly;
+    int      Nx;          /* ResolutionX */
+    float    hwr;         /* h_w / h     */
+    int      N1, N2;      /* MIS samples per target and sign (same for all instances) */
+    int      periodic;
+    int      law;         /* vpmc_law */
+    uint64_t seed;        /* Philox key; instance index is mixed in */
+} vpmc_sim_params;
+
+/* Create a simulation of `n_inst` independent instances (an ensemble; 1 for a
+ * single run).  counts[k] = particles of instance k; instances are stored
+ * back to back in the order given.  Mirrors Simulation(SimParam) +
+ * ParticleSet::resize (include/vortex_particle_mc.hpp:34-50,136-192). */
+int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms,
+                    const int* counts, vpmc_sim** out);
+int vpmc_sim_destroy(vpmc_sim* sim);
+int vpmc_sim_num_particles(vpmc_sim* sim);
+
+/* Upload positions (2N floats) and strengths (N floats).  is_host selects
+ * host or device source pointers.  omega may be NULL (left unchanged).
+ * Invalidates subsets/CDFs (rebuilt by vpmc_sim_prepare). */
+int vpmc_sim_set_particles(vpmc_sim* sim, const float* pos, const float* omega, int is_host);
+int vpmc_sim_get_particles(vpmc_sim* sim, float* pos, float* omega, float* vel, int is_host);
+
+/* Simulation::init's strength initialisation (src/vortex_particle_mc.cu:99-105,
+ * prepare_rhs_b :237-260, conjugate_gradient_rbf): b = omega_field (device,
+ * N floats; NULL = Taylor-Green 4 pi sin(2 pi x) sin(2 pi y), include/
+ * analytical_flow.hpp:24-28), solved per instance by vpmc_cg_rbf.
+ * info (HOST, may be NULL): 3 doubles per instance as vpmc_cg_rbf. */
+int vpmc_sim_init_strengths(vpmc_sim* sim, const float* omega_field, double tol,
+                            int max_iter, double* info);
+
+/* Sign subsets + FP64 |omega| CDFs + sampling tables for every instance
+ * (build_subsets_cuda).  Strengths are conserved, so this runs once after
+ * the strengths are set, not per step. */
+int vpmc_sim_prepare(vpmc_sim* sim);
+
+/* Simulation::step_cuda (src/cuda/simulation_step.cu:9-90) without the
+ * kernel deformation (aux=0, F=I): rebuild the hash, estimate
+ * u = u(+) - u(-) with the MIS estimator, x += dt*u, wrap x into the domain
+ * in FP64.  nsteps steps; the first call captures a CUDA graph per step
+ * shape and later calls replay it (use_graph != 0). */
+int vpmc_sim_step(vpmc_sim* sim, int nsteps, int use_graph);
+
+/* The MIS velocity at the current positions without moving them (for
+ * estimator checks).  vel: 2N floats, device.  `step` selects the Philox
+ * stream (the step counter is not advanced). */
+int vpmc_sim_velocity(vpmc_sim* sim, uint64_t step, float* vel);
+
+/* One step with host buffers: copies pos_in (2N) to the device, steps,
+ * copies positions and velocities back (2N each). */
+int vpmc_sim_step_host(vpmc_sim* sim, const float* pos_in, float* pos_out, float* vel_out);
+
+/* Change the estimator law / seed / step counter of an existing simulation. */
+int vpmc_sim_set_law(vpmc_sim* sim, int law);
+int vpmc_sim_set_seed(vpmc_sim* sim, uint64_t seed);
+int vpmc_sim_set_step(vpmc_sim* sim, uint64_t step);
+uint64_t vpmc_sim_get_step(vpmc_sim* sim);
+
+/* Neighbour-walk tuning: cells per h_w (k >= 1, walk (2k+1)^2 cells) and
+ * queries per thread in the field-evaluation kernel (1, 2 or 4).  0 = auto. */
+int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
+int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
+
+/* Kernels launched by the last vpmc_sim_step / vpmc_sim_velocity call (per
+ * step) and the device time of the field-evaluation kernel in it (ms). */
+int vpmc_sim_last_stats(vpmc_sim* sim, int* launches_per_step, float* eval_ms);
+
+/* ---------------------------------------------------------------- misc */
+/* Philox4x32-10 (Salmon et al., SC'11) block function, host evaluation:
+ * out[4] = philox(ctr[4], key[2]).  Exposed for known-answer tests. */
+void vpmc_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VPMC_H */

@@ -104,7 +104,7 @@ def lib():
             "orc_query_vorticity_f64": (None, [vp, vp, ip, ip, ip, ip, db, ip, vp]),
             "orc_field_exact_f64": (None, [vp, vp, ip, vp, ip, ip, ip, db, db, db, ip, vp]),
             "orc_mc_velocity": (None, [vp, vp, vp, ip, ip, ip, C.c_uint32, vp]),
-            "orc_mc_velocity_omp": (ip, [vp, vp, vp, ip, ip, ip, C.c_uint32, vp, ip]),
+            "orc_mc_velocity_omp": (ip, [vp, vp, vp, ip, ip, ip, C.c_uint32, vp, ip, ip, vp, ip]),
             "orc_rbf_matvec_f64": (None, [vp, vp, vp, db, ip, ip]),
             "orc_cg_rbf_f64": (ip, [vp, vp, vp, db, ip, db, ip, vp, vp, ip]),
             "orc_direct_mollified_f64": (None, [vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
@@ -392,12 +392,14 @@ def mc_velocity(state: OracleState, targets, N1, N2, seed):
     return vel
 
 
-def mc_velocity_omp(state: OracleState, targets, N1, N2, seed, nthreads=0):
+def mc_velocity_omp(state: OracleState, targets, N1, N2, seed, nthreads=0, law=0):
+    """law 0: monte_carlo_bs_cpu; law 1: the reference GPU kernel's sampling law."""
     t = np.ascontiguousarray(targets, np.float32)
     vel = np.zeros((len(t), 2), np.float32)
     ctx = state.mcctx()
+    tab = icdf(rcdf(state.prm.h_w, 20), state.prm.h_w)
     nt = lib().orc_mc_velocity_omp(C.byref(ctx), _ptr(state.pos), _ptr(t), len(t), N1, N2, seed,
-                                   _ptr(vel), nthreads)
+                                   _ptr(vel), nthreads, int(law), _ptr(tab), len(tab))
     return vel, nt
 
 

@@ -242,9 +242,29 @@ inline f2 mis_term(f2 dst, f2 sp, float om, float w1, float w2, float cum, float
 
 inline void add(f2& a, f2 b) { a.x += b.x; a.y += b.y; }
 
-// monte_carlo_bs_cpu, src/cpu/monte_carlo_bs.cpp:28-128.
+// mis_contrib_dev (src/cuda/monte_carlo_bs.cu:35-51): as mis_term but the
+// distance in alpha/r is the minimum image (wrap_delta, include/monte_carlo_bs.cuh:134-138).
+inline f2 mis_term_gpu(f2 dst, f2 sp, float om, float w1, float w2, float cum, float alpha,
+                       bool per, float Lx, float Ly) {
+    if (om <= 0.f) return f2{0.f, 0.f};
+    f2 r{dst.x - sp.x, dst.y - sp.y};
+    if (per) { r.x = r.x - std::round(r.x / Lx) * Lx; r.y = r.y - std::round(r.y / Ly) * Ly; }
+    const float rn = std::max(std::sqrt(r.x * r.x + r.y * r.y), 1e-6f);
+    const f2 k = bs_kernel(dst, sp);
+    const float denom = w1 * om / cum + w2 * alpha / rn;
+    const float s = om / denom;
+    return f2{k.x * s, k.y * s};
+}
+
+// monte_carlo_bs_cpu, src/cpu/monte_carlo_bs.cpp:28-128 (law 0), or the
+// sampling law of monte_carlo_bs_kernel_safe (src/cuda/monte_carlo_bs.cu:
+// 144-271) restated on the CPU with std::mt19937 (law 1): branch-1 jitter
+// radius interp(icdf)*h_w with icdf already scaled by h_w (include/
+// monte_carlo_bs.cuh:78-97, src/utilities.cu:87), the GPU query convention
+// (queryVorticityAbs, here in FP64) and minimum-image alpha/r.
 void mc_estimate(const orc_mcctx& C, const float* pos, const f2* dst, int sign,
-                 int aux, int N1, int N2, Rng& g, f2* out) {
+                 int aux, int N1, int N2, Rng& g, f2* out, int law = 0,
+                 const float* icdf = nullptr, int icdf_L = 0) {
     const float w1 = float(N1) / float(N1 + N2);
     const float w2 = float(N2) / float(N1 + N2);
     f2 s[5] = {};
@@ -267,6 +287,22 @@ void mc_estimate(const orc_mcctx& C, const float* pos, const f2* dst, int sign,
             sp.x += d.x * C.Lx;
             sp.y += d.y * C.Ly;
         }
+        if (law == 1) {
+            const float u = unif(g);
+            const float f = u * (icdf_L - 1);
+            const int i0 = int(f), i1 = std::min(i0 + 1, icdf_L - 1);
+            const float t = f - i0;
+            const float rr = (icdf[i0] * (1.f - t) + icdf[i1] * t) * C.h_w;
+            const float th = 2.f * kPiF * unif(g);
+            sp.x += rr * std::cos(th);
+            sp.y += rr * std::sin(th);
+            const float om = float(query_vort_f64(V, sp.x, sp.y, sign, false, false, C.h_w, per));
+            add(s[0], mis_term_gpu(dst[0], sp, om, w1, w2, cum, alpha_of(dst[0]), per, C.Lx, C.Ly));
+            if (aux)
+                for (int a = 1; a < 5; ++a)
+                    add(s[a], mis_term_gpu(dst[a], sp, om, w1, w2, cum, alpha_of(dst[a]), per, C.Lx, C.Ly));
+            continue;
+        }
         const float om = eval_vort_cpu(V, sp, sign, false, false, C.h_w, per);
         add(s[0], mis_term(dst[0], sp, om, w1, w2, cum, alpha_of(dst[0])));
         if (aux)
@@ -277,6 +313,11 @@ void mc_estimate(const orc_mcctx& C, const float* pos, const f2* dst, int sign,
             const float R = disk_radius(dst[a], per, C.Lx, C.Ly);
             const float al = 1.f / (2.f * kPiF * R);
             const f2 sp = sample_disk(g, dst[a], R);
+            if (law == 1) {
+                const float om = float(query_vort_f64(V, sp.x, sp.y, sign, false, false, C.h_w, per));
+                add(s[a], mis_term_gpu(dst[a], sp, om, w1, w2, cum, al, per, C.Lx, C.Ly));
+                continue;
+            }
             const float om = eval_vort_cpu(V, sp, sign, false, false, C.h_w, per);
             add(s[a], mis_term(dst[a], sp, om, w1, w2, cum, al));
         }
@@ -472,7 +513,8 @@ void orc_mc_velocity(const orc_mcctx* ctx, const float* pos, const float* target
 }
 
 int orc_mc_velocity_omp(const orc_mcctx* ctx, const float* pos, const float* targets,
-                        int M, int N1, int N2, uint32_t seed, float* vel, int nthreads) {
+                        int M, int N1, int N2, uint32_t seed, float* vel, int nthreads,
+                        int law, const float* icdf, int icdf_L) {
     const int nt = threads_or_default(nthreads);
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
     for (int t = 0; t < M; ++t) {
@@ -480,8 +522,8 @@ int orc_mc_velocity_omp(const orc_mcctx* ctx, const float* pos, const float* tar
         f2 dst[5];
         for (int a = 0; a < 5; ++a) dst[a] = ld2(targets, t);
         f2 vp[5], vn[5];
-        mc_estimate(*ctx, pos, dst, +1, 0, N1, N2, g, vp);
-        mc_estimate(*ctx, pos, dst, -1, 0, N1, N2, g, vn);
+        mc_estimate(*ctx, pos, dst, +1, 0, N1, N2, g, vp, law, icdf, icdf_L);
+        mc_estimate(*ctx, pos, dst, -1, 0, N1, N2, g, vn, law, icdf, icdf_L);
         vel[2 * t] = vp[0].x - vn[0].x;
         vel[2 * t + 1] = vp[0].y - vn[0].y;
     }

@@ -115,10 +115,15 @@ void orc_mc_velocity(const orc_mcctx* ctx, const float* pos,
                      uint32_t seed, float* vel);
 /* Same estimator, OpenMP over targets, target t seeded with seed + t (so the
  * result does not depend on the thread count).  Returns threads used.  This
- * parallel loop is harness-level: the reference's step_cpu is serial. */
+ * parallel loop is harness-level: the reference's step_cpu is serial.
+ * law 0 = monte_carlo_bs_cpu; law 1 = the sampling law of the reference's GPU
+ * kernel monte_carlo_bs_kernel_safe (jitter from `icdf` [icdf_L entries, as
+ * build_cubic_rcdf/cdf_to_icdf make it], GPU query convention in FP64,
+ * minimum-image alpha/r) restated with std::mt19937. */
 int  orc_mc_velocity_omp(const orc_mcctx* ctx, const float* pos,
                          const float* targets, int M, int N1, int N2,
-                         uint32_t seed, float* vel, int nthreads);
+                         uint32_t seed, float* vel, int nthreads,
+                         int law, const float* icdf, int icdf_L);
 
 /* ---- RBF system: src/cuda/cg_rbf_init.cu:11-116 restated in FP64 ---- */
 /* y = A x,  A_ij = W(|F_j^-1 (x_j - x_i)|) via the all-particle 3x3 walk. */

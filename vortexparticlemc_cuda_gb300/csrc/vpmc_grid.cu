@@ -1,0 +1,572 @@
+// vpmc_grid.cu -- evaluation grid: planning, stable build, query binning and
+// the field-evaluation kernel (the hot loop of queries, MIS samples and SpMV).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "vpmc_grid.cuh"
+
+namespace vpmc {
+
+namespace {
+
+constexpr int kEvalThreads = 256;
+constexpr int kMaxK = 4;
+constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
+constexpr int kCandCap = 2560;                 // float4 candidates staged per batch (40 KB)
+constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
+
+__device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].p_begin <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int inst_of_bin(const GridInst* inst, int n_inst, uint32_t b) {
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (uint32_t(inst[mid].bin_base) <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Wrap into [0, L) the way the reference does (p - floor(p/L)*L).
+__device__ __forceinline__ float wrapf(float p, float L) { return p - floorf(p / L) * L; }
+
+__global__ void k_grid_keys(const float2* __restrict__ pos, const float* __restrict__ omega, long n,
+                            const GridInst* __restrict__ inst, int n_inst, int set_mode, uint32_t nbins,
+                            uint32_t* __restrict__ keys, uint32_t* __restrict__ count) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const GridInst G = inst[inst_of_particle(inst, n_inst, i)];
+        const float w = omega ? omega[i] : 1.f;
+        int set = 0;
+        bool use = true;
+        switch (set_mode) {
+            case SET_SIGN_SPLIT: set = w > 0.f ? 0 : 1; use = w != 0.f; break;
+            case SET_POS_ONLY: use = w > 0.f; break;
+            case SET_NEG_ONLY: use = w < 0.f; break;
+            default: break;
+        }
+        uint32_t key = nbins;
+        if (use) {
+            float2 p = pos[i];
+            if (G.periodic) { p.x = wrapf(p.x, G.Lx); p.y = wrapf(p.y, G.Ly); }
+            const int cx = min(max(floor_int(p.x * G.inv_sx), 0), G.gx - 1);
+            const int cy = min(max(floor_int(p.y * G.inv_sy), 0), G.gy - 1);
+            key = uint32_t(G.bin_base) + uint32_t(set) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
+            atomicAdd(&count[key], 1u);
+        }
+        keys[i] = key;
+    }
+}
+
+__global__ void k_grid_gather(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ start, long n,
+                              uint32_t nbins, const float2* __restrict__ pos, const float* __restrict__ omega,
+                              const GridInst* __restrict__ inst, int n_inst, int set_mode,
+                              float4* __restrict__ cand) {
+    const long nv = start[nbins];
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x) {
+        const uint32_t i = perm[p];
+        const GridInst G = inst[inst_of_particle(inst, n_inst, i)];
+        float2 q = pos[i];
+        if (G.periodic) { q.x = wrapf(q.x, G.Lx); q.y = wrapf(q.y, G.Ly); }
+        const float w = omega ? omega[i] : 1.f;
+        const float wt = (set_mode == SET_ONE_SIGNED ? w : fabsf(w)) * G.two_sigma;
+        cand[p] = make_float4(q.x, q.y, wt, 0.f);
+    }
+}
+
+__global__ void k_grid_weights(const double* __restrict__ x, long n, double scale, float4* __restrict__ cand) {
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += long(gridDim.x) * blockDim.x) {
+        const double v = x[p] * scale;
+        const float hi = float(v);
+        cand[p].z = hi;
+        cand[p].w = float(v - double(hi));
+    }
+}
+
+__global__ void k_bin_points(const float2* __restrict__ pts, long M, const GridInst* __restrict__ inst,
+                             int set, int field9, uint32_t* __restrict__ qbin, uint32_t* __restrict__ qcount) {
+    for (long m = long(blockIdx.x) * blockDim.x + threadIdx.x; m < M; m += long(gridDim.x) * blockDim.x) {
+        const GridInst G = inst[0];
+        float2 p = pts[m];
+        uint32_t b = kNoBin;
+        bool ok = p.x == p.x && p.y == p.y;
+        if (ok && G.periodic) {
+            const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+            if (field9 && (fabsf(kx) > 2.f || fabsf(ky) > 2.f)) ok = false;
+            p.x = p.x - kx * G.Lx;
+            p.y = p.y - ky * G.Ly;
+        } else if (ok) {
+            ok = !(p.x < 0.f || p.x > G.Lx || p.y < 0.f || p.y > G.Ly);
+        }
+        if (ok) {
+            const int cx = min(max(floor_int(p.x * G.inv_sx), 0), G.gx - 1);
+            const int cy = min(max(floor_int(p.y * G.inv_sy), 0), G.gy - 1);
+            b = uint32_t(G.bin_base) + uint32_t(set) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
+            atomicAdd(&qcount[b], 1u);
+        }
+        qbin[m] = b;
+    }
+}
+
+__global__ void k_scatter_points(const float2* __restrict__ pts, long M, const GridInst* __restrict__ inst,
+                                 int n_inst, const uint32_t* __restrict__ qbin, const uint32_t* __restrict__ qstart,
+                                 uint32_t* __restrict__ qfill, QRec* __restrict__ qrec) {
+    for (long m = long(blockIdx.x) * blockDim.x + threadIdx.x; m < M; m += long(gridDim.x) * blockDim.x) {
+        const uint32_t b = qbin[m];
+        if (b == kNoBin) continue;
+        const GridInst G = inst[inst_of_bin(inst, n_inst, b)];
+        float2 p = pts[m];
+        uint32_t fl = (2u) | (2u << 3);
+        if (G.periodic) {
+            const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+            p.x = p.x - kx * G.Lx;
+            p.y = p.y - ky * G.Ly;
+            const int ikx = min(max(int(kx), -2), 2), iky = min(max(int(ky), -2), 2);
+            fl = uint32_t(ikx + 2) | (uint32_t(iky + 2) << 3);
+        }
+        const uint32_t slot = atomicAdd(&qfill[b], 1u);
+        qrec[qstart[b] + slot] = QRec{p.x, p.y, uint32_t(m), fl};
+    }
+}
+
+__global__ void k_items_count(const uint32_t* __restrict__ qstart, long nbins, int chunk,
+                              uint32_t* __restrict__ per_bin) {
+    for (long b = long(blockIdx.x) * blockDim.x + threadIdx.x; b < nbins; b += long(gridDim.x) * blockDim.x) {
+        const uint32_t c = qstart[b + 1] - qstart[b];
+        per_bin[b] = (c + chunk - 1) / chunk;
+    }
+}
+
+__global__ void k_items_fill(const uint32_t* __restrict__ qstart, long nbins, int chunk,
+                             const uint32_t* __restrict__ item_start, const GridInst* __restrict__ inst,
+                             int n_inst, Item* __restrict__ items, uint32_t* __restrict__ n_items,
+                             uint32_t* __restrict__ counter, long max_items) {
+    for (long b = long(blockIdx.x) * blockDim.x + threadIdx.x; b < nbins; b += long(gridDim.x) * blockDim.x) {
+        const uint32_t q0 = qstart[b], c = qstart[b + 1] - q0;
+        uint32_t it = item_start[b];
+        const uint32_t ib = uint32_t(inst_of_bin(inst, n_inst, uint32_t(b)));
+        for (uint32_t o = 0; o < c; o += chunk, ++it)
+            if (it < max_items) items[it] = Item{uint32_t(b), q0 + o, min(uint32_t(chunk), c - o), ib};
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint32_t t = item_start[nbins];
+        *n_items = t < max_items ? t : uint32_t(max_items);
+        *counter = 0;
+    }
+}
+
+// ---------------------------------------------------------------- eval kernel
+struct Piece {
+    uint32_t gstart, cnt;   // candidate run in global memory
+    float qdx, qdy;         // offset added to the query point (folds the periodic image)
+    int mx, my;             // image index of the run (for FIELD9)
+};
+struct BatchPiece {
+    uint32_t soff, cnt, gstart;
+    int piece;
+};
+
+struct EvalArgs {
+    const GridInst* inst;
+    const uint32_t* cstart;
+    const float4* cand;
+    const QRec* qrec;
+    const Item* items;
+    const uint32_t* n_items;
+    uint32_t* counter;
+    float* out_f32;
+    double* out_f64;
+    unsigned* flags;
+};
+
+template <int MODE, int QPT>
+__global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
+    extern __shared__ __align__(128) float4 s_cand[];
+    __shared__ Piece s_pc[kMaxPieces];
+    __shared__ BatchPiece s_bp[kMaxPieces + 2];
+    __shared__ int s_np, s_nbp, s_cur_piece, s_abort;
+    __shared__ uint32_t s_cur_off, s_btot, s_item;
+    __shared__ __align__(8) uint64_t s_bar;
+
+    constexpr bool kF64 = MODE == EVAL_SPMV64;
+    constexpr bool kComp = MODE == EVAL_SPMV32;
+    using Acc = typename std::conditional<kF64, double, float>::type;
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= *a.n_items) break;
+        const Item it = a.items[item];
+        const GridInst G = a.inst[it.inst];
+
+        if (tid == 0) {
+            const uint32_t local = it.bin - uint32_t(G.bin_base);
+            const uint32_t ncell = uint32_t(G.gx * G.gy);
+            const uint32_t set = local / ncell, cell = local % ncell;
+            const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
+            const uint32_t colbase = uint32_t(G.bin_base) + set * ncell;
+            int np = 0;
+            auto add = [&](int gxx, int r0, int r1, int sxi, int syi) {
+                if (r0 > r1) return;
+                const uint32_t b0 = colbase + uint32_t(gxx * G.gy + r0);
+                const uint32_t s = a.cstart[b0], e = a.cstart[b0 + uint32_t(r1 - r0) + 1];
+                if (e > s && np < kMaxPieces)
+                    s_pc[np++] = Piece{s, e - s, -float(sxi) * G.Lx, -float(syi) * G.Ly, sxi, syi};
+            };
+            for (int ox = -G.k; ox <= G.k; ++ox) {
+                int gxx = cx + ox, sxi = 0;
+                if (G.periodic) {
+                    if (gxx < 0) { gxx += G.gx; sxi = -1; }
+                    else if (gxx >= G.gx) { gxx -= G.gx; sxi = 1; }
+                } else if (gxx < 0 || gxx >= G.gx) {
+                    continue;
+                }
+                const int ylo = cy - G.k, yhi = cy + G.k;
+                if (G.periodic) {
+                    if (ylo < 0) { add(gxx, 0, yhi, sxi, 0); add(gxx, ylo + G.gy, G.gy - 1, sxi, -1); }
+                    else if (yhi >= G.gy) { add(gxx, ylo, G.gy - 1, sxi, 0); add(gxx, 0, yhi - G.gy, sxi, 1); }
+                    else add(gxx, ylo, yhi, sxi, 0);
+                } else {
+                    add(gxx, max(ylo, 0), min(yhi, G.gy - 1), 0, 0);
+                }
+            }
+            s_np = np;
+            s_cur_piece = 0;
+            s_cur_off = 0;
+        }
+
+        // this thread's queries
+        float qx[QPT], qy[QPT];
+        uint32_t qid[QPT];
+        int qmx[QPT], qmy[QPT];
+        bool qv[QPT];
+        Acc acc[QPT];
+        float acc_c[QPT];
+#pragma unroll
+        for (int j = 0; j < QPT; ++j) {
+            const uint32_t idx = uint32_t(tid + j * kEvalThreads);
+            qv[j] = idx < it.qcnt;
+            QRec r = qv[j] ? a.qrec[it.qbeg + idx] : QRec{0.f, 0.f, 0u, (2u) | (2u << 3)};
+            qx[j] = r.x;
+            qy[j] = r.y;
+            qid[j] = r.id;
+            qmx[j] = int(r.flags & 7u) - 2;
+            qmy[j] = int((r.flags >> 3) & 7u) - 2;
+            acc[j] = Acc(0);
+            acc_c[j] = 0.f;
+        }
+        __syncthreads();
+
+        for (;;) {
+            if (tid == 0) {
+                // next batch: whole or partial pieces up to the staging capacity
+                int pc = s_cur_piece;
+                uint32_t po = s_cur_off, tot = 0;
+                int nb = 0;
+                while (pc < s_np && tot < uint32_t(kCandCap) && nb < kMaxPieces + 2) {
+                    const uint32_t rem = s_pc[pc].cnt - po;
+                    const uint32_t take = min(rem, uint32_t(kCandCap) - tot);
+                    s_bp[nb++] = BatchPiece{tot, take, s_pc[pc].gstart + po, pc};
+                    tot += take;
+                    po += take;
+                    if (po == s_pc[pc].cnt) { ++pc; po = 0; }
+                }
+                s_cur_piece = pc;
+                s_cur_off = po;
+                s_nbp = nb;
+                s_btot = tot;
+                if (tot > 0) {
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(&s_bar, tot * 16u);
+                    for (int b = 0; b < nb; ++b)
+                        bulk_g2s(&s_cand[s_bp[b].soff], &a.cand[s_bp[b].gstart], s_bp[b].cnt * 16u, &s_bar);
+                }
+            }
+            __syncthreads();
+            if (s_btot == 0) break;
+            if (!mbar_wait_bounded(&s_bar, phase, kWaitLimit)) atomicOr(&s_abort, 1);
+            phase ^= 1u;
+            __syncthreads();
+            if (s_abort) break;
+
+            const int nbp = s_nbp;
+            for (int b = 0; b < nbp; ++b) {
+                const BatchPiece bp = s_bp[b];
+                const Piece pc = s_pc[bp.piece];
+                float px[QPT], py[QPT];
+                Acc part[QPT];
+#pragma unroll
+                for (int j = 0; j < QPT; ++j) {
+                    px[j] = qx[j] + pc.qdx;
+                    py[j] = qy[j] + pc.qdy;
+                    part[j] = Acc(0);
+                }
+                const float4* cs = s_cand + bp.soff;
+                const int cnt = int(bp.cnt);
+                if constexpr (kF64) {
+                    const double hw = double(G.hw);
+                    const float lim = G.hw * G.hw * 1.0001f;
+#pragma unroll 2
+                    for (int c = 0; c < cnt; ++c) {
+                        const float4 cv = cs[c];
+#pragma unroll
+                        for (int j = 0; j < QPT; ++j) {
+                            const float dx = cv.x - px[j], dy = cv.y - py[j];
+                            if (dx * dx + dy * dy < lim) {
+                                const double ddx = double(cv.x) - (double(qx[j]) + double(pc.qdx));
+                                const double ddy = double(cv.y) - (double(qy[j]) + double(pc.qdy));
+                                const double r = sqrt(ddx * ddx + ddy * ddy);
+                                part[j] += (double(cv.z) + double(cv.w)) * spline_w_d(r, hw);
+                            }
+                        }
+                    }
+                } else {
+                    const float A = G.A, B = G.B, ih = G.inv_hw;
+#pragma unroll 4
+                    for (int c = 0; c < cnt; ++c) {
+                        const float4 cv = cs[c];
+#pragma unroll
+                        for (int j = 0; j < QPT; ++j) {
+                            const float dx = cv.x - px[j], dy = cv.y - py[j];
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, 1e-30f));
+                            const float r = r2 * rsqrtf(r2);
+                            const float inner = fmaf(r2, fmaf(A, r, B), 0.5f);
+                            const float t = fmaf(-ih, r, 1.0f);
+                            float v = fmaxf(fminf(inner, t * t * t), 0.0f);
+                            if (MODE == EVAL_FIELD_EXC && r2 < 1e-12f) v = 0.f;
+                            part[j] = fmaf(cv.z, v, part[j]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < QPT; ++j) {
+                    bool use = true;
+                    if (MODE == EVAL_FIELD9) {
+                        const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
+                        use = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
+                    }
+                    if (use) {
+                        if constexpr (kComp) {
+                            // compensated accumulation of the per-run partial sums
+                            const float y = float(part[j]) - acc_c[j];
+                            const float tt = float(acc[j]) + y;
+                            acc_c[j] = (tt - float(acc[j])) - y;
+                            acc[j] = tt;
+                        } else {
+                            acc[j] += part[j];
+                        }
+                    }
+                }
+            }
+            __syncthreads();   // all reads of s_cand done before the next batch overwrites it
+        }
+        if (s_abort) break;
+#pragma unroll
+        for (int j = 0; j < QPT; ++j) {
+            if (!qv[j]) continue;
+            if constexpr (kF64) a.out_f64[qid[j]] = acc[j];
+            else if constexpr (kComp) a.out_f64[qid[j]] = double(acc[j]) - double(acc_c[j]);
+            else a.out_f32[qid[j]] = acc[j];
+        }
+        __syncthreads();
+    }
+    if (s_abort) {
+        if (tid == 0) {
+            atomicOr(a.flags, FLAG_TIMEOUT);
+            (void)mbar_wait_bounded(&s_bar, phase ^ 1u, kWaitLimit);   // let an in-flight copy land
+        }
+    }
+}
+
+template <int MODE, int QPT>
+int launch_eval_t(vpmc_context* ctx, const EvalArgs& a) {
+    const size_t smem = size_t(kCandCap) * sizeof(float4);
+    static bool configured[64] = {};
+    const int dev = ctx->device;
+    if (dev < 64 && !configured[dev]) {
+        VPMC_CUDA(cudaFuncSetAttribute(k_eval<MODE, QPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        configured[dev] = true;
+    }
+    int per_sm = 0;
+    VPMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<MODE, QPT>, kEvalThreads, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int grid = ctx->sm_count * per_sm;
+    VPMC_LAUNCH((k_eval<MODE, QPT>), grid, kEvalThreads, smem, ctx->stream, a);
+    return VPMC_OK;
+}
+
+int blocks_for(long n, int threads = 256) {
+    long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 65535L * 16) b = 65535L * 16;
+    return int(b);
+}
+
+}  // namespace
+
+int default_k() { return 2; }
+
+int query_chunk(int qpt) { return (qpt == 1 || qpt == 2 ? qpt : 4) * kEvalThreads; }
+
+long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
+    if (k <= 0) k = default_k();
+    if (k > kMaxK) k = kMaxK;
+    long base = 0;
+    for (int i = 0; i < n; ++i) {
+        const InstDesc& d = in[i];
+        if (!(d.hw > 0.f) || !(d.Lx > 0.f) || !(d.Ly > 0.f)) return -VPMC_ERR_INVALID;
+        int kk = k, gx = 0, gy = 0;
+        for (; kk >= 1; --kk) {
+            gx = int(std::floor(double(kk) * double(d.Lx) / double(d.hw) + 1e-9));
+            gy = int(std::floor(double(kk) * double(d.Ly) / double(d.hw) + 1e-9));
+            if (!d.periodic || (gx >= 2 * kk + 1 && gy >= 2 * kk + 1)) break;
+        }
+        if (kk < 1 || gx < 1 || gy < 1) return -VPMC_ERR_GEOMETRY;
+        if (long(gx) * gy > (1L << 24)) return -VPMC_ERR_CAPACITY;
+        GridInst g{};
+        g.Lx = d.Lx;
+        g.Ly = d.Ly;
+        g.gx = gx;
+        g.gy = gy;
+        g.inv_sx = float(gx) / d.Lx;
+        g.inv_sy = float(gy) / d.Ly;
+        g.k = kk;
+        g.bin_base = int(base);
+        g.nsets = nsets;
+        g.periodic = d.periodic;
+        g.hw = d.hw;
+        const double h = d.hw;
+        g.inv_hw = float(1.0 / h);
+        g.A = float(3.0 / (h * h * h));
+        g.B = float(-3.0 / (h * h));
+        g.two_sigma = float(2.0 * 40.0 / (7.0 * kPiD * h * h));
+        g.p_begin = d.p_begin;
+        g.p_end = d.p_end;
+        out[i] = g;
+        base += long(nsets) * gx * gy;
+        if (base >= (1L << 31)) return -VPMC_ERR_CAPACITY;
+    }
+    return base;
+}
+
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g) {
+    g->inst = c.take<GridInst>(size_t(n_inst));
+    g->n_inst = n_inst;
+    g->nbins = nbins;
+    g->n = n;
+    g->keys = c.take<uint32_t>(size_t(n < 1 ? 1 : n));
+    g->count = c.take<uint32_t>(size_t(nbins + 1));
+    g->start = c.take<uint32_t>(size_t(nbins + 1));
+    g->cand = c.take<float4>(size_t(n < 1 ? 1 : n));
+    carve_radix(c, n, &g->rs);
+    // the bin scan reuses the radix scan scratch when it is large enough
+    const size_t need = scan_tmp_elems(nbins + 1);
+    if (need > scan_tmp_elems(long(radix_counts_elems(n)))) g->rs.scan_tmp = c.take<uint32_t>(need + 1);
+}
+
+int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode) {
+    cudaStream_t st = ctx->stream;
+    VPMC_CUDA(cudaMemsetAsync(g.count, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
+    VPMC_LAUNCH(k_grid_keys, blocks_for(g.n), 256, 0, st, pos, omega, g.n, g.inst, g.n_inst, set_mode,
+                uint32_t(g.nbins), g.keys, g.count);
+    VPMC_TRY(exclusive_scan(ctx, g.count, g.start, g.nbins, g.rs.scan_tmp, true));
+    uint32_t *ks = nullptr, *vs = nullptr;
+    VPMC_TRY(radix_sort(ctx, g.keys, nullptr, g.n, bits_for(uint64_t(g.nbins) + 1), g.rs, &ks, &vs));
+    g.perm = vs;
+    VPMC_LAUNCH(k_grid_gather, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega,
+                g.inst, g.n_inst, set_mode, g.cand);
+    return VPMC_OK;
+}
+
+int grid_set_weights_sorted(vpmc_context* ctx, GridBufs& g, const double* x_sorted, double scale) {
+    VPMC_LAUNCH(k_grid_weights, blocks_for(g.n), 256, 0, ctx->stream, x_sorted, g.n, scale, g.cand);
+    return VPMC_OK;
+}
+
+void carve_items(Carver& c, long nbins, long max_queries, ItemBufs* it) {
+    it->max_items = max_queries / query_chunk(1) + nbins + 1;
+    it->items = c.take<Item>(size_t(it->max_items));
+    it->n_items = c.take<uint32_t>(1);
+    it->counter = c.take<uint32_t>(1);
+    it->per_bin = c.take<uint32_t>(size_t(nbins + 1));
+    it->item_start = c.take<uint32_t>(size_t(nbins + 1));
+    it->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
+}
+
+int make_items(vpmc_context* ctx, const GridBufs& g, const uint32_t* qstart, ItemBufs& it, int chunk) {
+    cudaStream_t st = ctx->stream;
+    VPMC_LAUNCH(k_items_count, blocks_for(g.nbins), 256, 0, st, qstart, g.nbins, chunk, it.per_bin);
+    VPMC_TRY(exclusive_scan(ctx, it.per_bin, it.item_start, g.nbins, it.scan_tmp, true));
+    VPMC_LAUNCH(k_items_fill, blocks_for(g.nbins), 256, 0, st, qstart, g.nbins, chunk, it.item_start, g.inst,
+                g.n_inst, it.items, it.n_items, it.counter, it.max_items);
+    return VPMC_OK;
+}
+
+void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q) {
+    const size_t m = size_t(max_points < 1 ? 1 : max_points);
+    q->qbin = c.take<uint32_t>(m);
+    q->qcount = c.take<uint32_t>(size_t(nbins + 1));
+    q->qstart = c.take<uint32_t>(size_t(nbins + 1));
+    q->qfill = c.take<uint32_t>(size_t(nbins + 1));
+    q->qrec = c.take<QRec>(m);
+    q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
+}
+
+int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M, int field9) {
+    (void)field9;
+    cudaStream_t st = ctx->stream;
+    VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
+    VPMC_CUDA(cudaMemsetAsync(q.qfill, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
+    VPMC_LAUNCH(k_scatter_points, blocks_for(M), 256, 0, st, pts, M, g.inst, g.n_inst, q.qbin, q.qstart, q.qfill,
+                q.qrec);
+    return VPMC_OK;
+}
+
+int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M, int set, int field9) {
+    cudaStream_t st = ctx->stream;
+    VPMC_CUDA(cudaMemsetAsync(q.qcount, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
+    VPMC_LAUNCH(k_bin_points, blocks_for(M), 256, 0, st, pts, M, g.inst, set, field9, q.qbin, q.qcount);
+    return scatter_points(ctx, g, q, pts, M, field9);
+}
+
+int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
+    EvalArgs a{g.inst, g.start, g.cand, qrec, it.items, it.n_items, it.counter, L.out_f32, L.out_f64, ctx->d_flags};
+    switch (L.mode) {
+        case EVAL_FIELD:
+            if (L.qpt == 1) return launch_eval_t<EVAL_FIELD, 1>(ctx, a);
+            if (L.qpt == 2) return launch_eval_t<EVAL_FIELD, 2>(ctx, a);
+            return launch_eval_t<EVAL_FIELD, 4>(ctx, a);
+        case EVAL_FIELD9:
+            if (L.qpt == 1) return launch_eval_t<EVAL_FIELD9, 1>(ctx, a);
+            if (L.qpt == 2) return launch_eval_t<EVAL_FIELD9, 2>(ctx, a);
+            return launch_eval_t<EVAL_FIELD9, 4>(ctx, a);
+        case EVAL_FIELD_EXC:
+            if (L.qpt != 4) return VPMC_ERR_INVALID;
+            return launch_eval_t<EVAL_FIELD_EXC, 4>(ctx, a);
+        case EVAL_SPMV64:
+            if (L.qpt != 4) return VPMC_ERR_INVALID;
+            return launch_eval_t<EVAL_SPMV64, 4>(ctx, a);
+        case EVAL_SPMV32:
+            if (L.qpt != 4) return VPMC_ERR_INVALID;
+            return launch_eval_t<EVAL_SPMV32, 4>(ctx, a);
+        default: return VPMC_ERR_INVALID;
+    }
+}
+
+}  // namespace vpmc

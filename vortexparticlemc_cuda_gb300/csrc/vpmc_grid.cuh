@@ -1,0 +1,145 @@
+// vpmc_grid.cuh -- cell-binned particle sets and the field-evaluation kernel.
+//
+// Every field query in the library (vorticity queries, MIS sample values, the
+// RBF SpMV) runs through the same structure:
+//   * particles ("candidates") are sorted stably by bin = (instance, sign set,
+//     cell) on a grid whose cell side s >= h_w / k, and gathered into an AoS
+//     float4 {x, y, weight, weight_lo} array so each cell is one contiguous run;
+//   * query points are binned by the cell of their wrapped position;
+//   * one CTA takes a bin (or a chunk of it), stages the (2k+1)^2 neighbour
+//     cells -- at most 2(2k+1) contiguous runs, one per column and periodic
+//     wrap -- into shared memory with bulk (TMA) copies, and evaluates every
+//     query of the bin against them.  Periodic images are folded into a
+//     per-run offset of the query point, so the inner loop has no branches.
+#pragma once
+
+#include "vpmc_internal.cuh"
+
+namespace vpmc {
+
+// Geometry of one instance on the evaluation grid (device visible).
+struct GridInst {
+    float Lx, Ly;
+    float inv_sx, inv_sy;   // gx/Lx, gy/Ly
+    int gx, gy;             // cells per axis
+    int k;                  // walk half width in cells
+    int bin_base;           // first bin of the instance
+    int nsets;              // candidate sets (2 = sign split, 1 = one set)
+    int periodic;
+    float hw;               // support radius h_w
+    float inv_hw;           // 1/h_w
+    float A, B;             // 3/h_w^3, -3/h_w^2: W/(2 sigma) = min(0.5 + r^2 (A r + B), (1 - r/h_w)^3)
+    float two_sigma;        // 2 * 40 / (7 pi h_w^2)
+    int p_begin, p_end;     // particle range of the instance
+};
+
+// Query record: wrapped position, output slot, image flags (16 bytes).
+struct QRec {
+    float x, y;
+    uint32_t id;
+    uint32_t flags;   // bits 0-2: kx+2, bits 3-5: ky+2 (unwrapped image of the point)
+};
+
+struct Item {
+    uint32_t bin;
+    uint32_t qbeg;
+    uint32_t qcnt;
+    uint32_t inst;
+};
+
+enum EvalMode : int {
+    EVAL_FIELD = 0,      // out_f32[id] = sum w W          (periodic / plain field)
+    EVAL_FIELD9 = 1,     // as FIELD, only images m in {-1,0,1}^2 of the unwrapped point
+    EVAL_FIELD_EXC = 2,  // as FIELD, pairs closer than 1e-6 skipped (exclude_center)
+    EVAL_SPMV64 = 3,     // out_f64[id] = sum (w + w_lo) W, in-support pairs in FP64
+    EVAL_SPMV32 = 4,     // out_f64[id] = compensated FP32 sum
+};
+
+enum SetMode : int {
+    SET_SIGN_SPLIT = 0,  // set 0: omega > 0, set 1: omega < 0; weight |omega| * 2 sigma
+    SET_ONE_SIGNED = 1,  // one set, all particles; weight omega (value or external vector)
+    SET_POS_ONLY = 2,    // one set, omega > 0
+    SET_NEG_ONLY = 3,    // one set, omega < 0
+    SET_ONE_ABS = 4,     // one set, all particles; weight |omega|
+};
+
+constexpr uint32_t kNoBin = 0xffffffffu;
+
+// Host description of an instance before planning.
+struct InstDesc {
+    float Lx, Ly, hw;
+    int periodic;
+    int p_begin, p_end;
+};
+
+// Plan the grid: fills `out` (n entries) and returns the bin count, or a
+// negative vpmc_status on geometry errors.  k <= 0 selects the default.
+long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out);
+int default_k();
+
+// Device-side working set of one grid (caller owns the memory).
+struct GridBufs {
+    GridInst* inst = nullptr;   // device copy of the plan
+    int n_inst = 0;
+    long nbins = 0;
+    long n = 0;                 // particles covered
+    uint32_t* keys = nullptr;   // n
+    uint32_t* count = nullptr;  // nbins + 1
+    uint32_t* start = nullptr;  // nbins + 1 (exclusive prefix, start[nbins] = candidates)
+    float4* cand = nullptr;     // n
+    uint32_t* perm = nullptr;   // n: sorted slot -> particle (points into rs buffers)
+    RadixScratch rs{};
+};
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g);
+
+// Bin keys + counts + stable sort + ranges + gather.  weights == nullptr uses
+// omega (SET_SIGN_SPLIT scales |omega| by 2 sigma, SET_ONE_SIGNED by
+// 2 sigma too).  Writes g.cand / g.start / g.perm.
+int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode);
+// Overwrite candidate weights from a vector in sorted order: cand[p].z/.w =
+// hi/lo FP32 split of scale * x[p] (FP64 in, for the SpMV).
+int grid_set_weights_sorted(vpmc_context* ctx, GridBufs& g, const double* x_sorted, double scale);
+
+// Work items for queries that are already grouped by bin: qstart[b]..qstart[b+1].
+struct ItemBufs {
+    Item* items = nullptr;
+    uint32_t* n_items = nullptr;    // device scalar
+    uint32_t* per_bin = nullptr;    // nbins + 1
+    uint32_t* item_start = nullptr; // nbins + 1
+    uint32_t* counter = nullptr;    // work counter (device scalar)
+    uint32_t* scan_tmp = nullptr;
+    long max_items = 0;
+};
+void carve_items(Carver& c, long nbins, long max_queries, ItemBufs* it);
+// chunk = queries per item = 256 * queries-per-thread of the eval launch.
+int make_items(vpmc_context* ctx, const GridBufs& g, const uint32_t* qstart, ItemBufs& it, int chunk);
+int query_chunk(int qpt);
+
+// Query binning for points/samples: bin ids (kNoBin = skip) -> counts -> scan
+// -> scatter into QRec by bin (order inside a bin is irrelevant).
+struct QueryBufs {
+    uint32_t* qbin = nullptr;    // per point
+    uint32_t* qcount = nullptr;  // nbins + 1
+    uint32_t* qstart = nullptr;  // nbins + 1
+    uint32_t* qfill = nullptr;   // nbins
+    QRec* qrec = nullptr;        // max points
+    uint32_t* scan_tmp = nullptr;
+};
+void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q);
+// Bin arbitrary points (one instance `inst_of` lookup per point by index range
+// `point_inst` == nullptr -> instance 0).  set = candidate set to query.
+int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M, int set,
+               int field9);
+// Scatter points whose bins are already in q.qbin (counts in q.qcount).
+int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M,
+                   int field9);
+
+struct EvalLaunch {
+    int mode = EVAL_FIELD;
+    int qpt = 4;               // queries per thread (1, 2, 4)
+    float* out_f32 = nullptr;
+    double* out_f64 = nullptr;
+};
+int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L);
+
+}  // namespace vpmc

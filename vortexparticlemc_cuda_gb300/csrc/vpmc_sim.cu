@@ -1,0 +1,812 @@
+// vpmc_sim.cu -- the simulation handle: MIS Monte-Carlo Biot-Savart velocity
+// with advection (Simulation::step_cuda, src/cuda/simulation_step.cu:9-90;
+// monte_carlo_bs_kernel_safe, src/cuda/monte_carlo_bs.cu:144-271), batched
+// over instances (ensembles), captured as one CUDA graph per step.
+//
+// Per step:
+//   1. grid: particles -> bins (instance, sign, cell), stable sort, candidate
+//      runs {x, y, |omega| 2 sigma} (vpmc_grid.cu);
+//   2. per chunk of targets:
+//      gen     one thread per (target, sign, sample): Philox4x32-10 keyed by
+//              (seed, instance) with counter (sample|sign, target, step) ->
+//              branch 1: |omega| CDF (FP64, guide table + binary search),
+//              image tile, kernel jitter; branch 2: disk draw.  Writes the
+//              sample point and its bin;
+//      bin     counts -> scan -> scatter into per-bin query records;
+//      eval    field value at every sample (vpmc_grid.cu k_eval);
+//      accum   one warp per target: MIS terms, Kahan-compensated FP32 sums in
+//              a fixed order, u = u(+) - u(-), x += dt u with an FP64 wrap.
+//   Results do not depend on scheduling: each sample's field value is a fixed
+//   ordered sum and every reduction has a fixed tree.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "vpmc_grid.cuh"
+
+namespace vpmc {
+
+int build_subsets_dev(vpmc_context* ctx, long N, const float* omega, int* sub_pos, int* sub_neg, double* cdf_pos,
+                      double* cdf_neg, float* c32p, float* c32n, int* cnt, double* cum);
+
+namespace {
+
+constexpr int kIcdfRef = 20;      // reference iCDF table length (src/vortex_particle_mc.cu:89)
+constexpr int kJitTab = 1024;     // inverse spline-radius CDF table (unbiased law)
+
+struct InstMC {
+    float Lx, Ly, hw, dt;
+    int periodic, law;
+    float cum9[2];         // Omega_s (x9 when periodic), FP32 copy of the FP64 totals
+    int cnt[2];
+    long off[2];           // offsets of the subset in sub/cdf/guide arrays
+    long goff[2];          // guide table offsets (cnt+2 entries each)
+    uint32_t key0, key1;   // Philox key
+    int p_begin, p_end;
+    float icdf[kIcdfRef];  // reference law: r = interp(icdf) * h_w
+};
+
+__device__ __forceinline__ int inst_of(const InstMC* I, int n, long t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (I[mid].p_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// SamplingDiskRadius (include/monte_carlo_bs.hpp:73-89), same FP32 steps.
+__host__ __device__ __forceinline__ float disk_radius(float2 d, bool periodic, float Lx, float Ly) {
+    if (!periodic) return sqrtf(Lx * Lx + Ly * Ly);
+    float m = 0.f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy) {
+            const float ix = d.x + dx * Lx, iy = d.y + dy * Ly;
+            const float ex = ix - d.x, ey = iy - d.y;
+            m = fmaxf(m, ex * ex + ey * ey);
+        }
+    return sqrtf(m);
+}
+
+// upper_bound(cdf[0..n), u) bracketed by a guide table of G = n entries:
+// guide[k] = upper_bound(k / G); result clamped to n-1 as the reference does.
+__device__ __forceinline__ int sample_cdf(const double* __restrict__ cdf, const uint32_t* __restrict__ guide, int n,
+                                          double u) {
+    const int G = n;
+    int k = int(u * G);
+    k = min(max(k, 0), G - 1);
+    int lo = int(guide[max(k - 1, 0)]);
+    int hi = int(guide[min(k + 2, G)]);   // guide[G] = n
+    // first index in [lo, hi) with cdf > u
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] > u) hi = mid; else lo = mid + 1;
+    }
+    return min(lo, n - 1);
+}
+
+__global__ void k_guide(const double* __restrict__ cdf, int n, uint32_t* __restrict__ guide) {
+    for (long k = long(blockIdx.x) * blockDim.x + threadIdx.x; k <= n; k += long(gridDim.x) * blockDim.x) {
+        const double v = double(k) / double(n);
+        int lo = 0, hi = n;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (cdf[mid] > v) hi = mid; else lo = mid + 1;
+        }
+        guide[k] = uint32_t(k == n ? n : lo);
+    }
+}
+
+struct GenArgs {
+    const InstMC* mc;
+    int n_inst;
+    const GridInst* gi;
+    const float2* pos;
+    const float4* F;              // unused (F = I on this path)
+    const int* sub;
+    const double* cdf;
+    const uint32_t* guide;
+    const float* jit;             // kJitTab+1 entries: inverse spline-radius CDF (units of h_w)
+    const unsigned long long* step;
+    long t0, nt;                  // target chunk
+    int N1, N2;
+    float2* ys;
+    uint32_t* qbin;
+    uint32_t* qcount;
+};
+
+__global__ void __launch_bounds__(256) k_gen(GenArgs a) {
+    const int Q = a.N1 + a.N2;
+    const long total = a.nt * 2 * Q;
+    const unsigned long long step = *a.step;
+    for (long sid = long(blockIdx.x) * blockDim.x + threadIdx.x; sid < total; sid += long(gridDim.x) * blockDim.x) {
+        const long tl = sid / (2 * Q);
+        const int rem = int(sid - tl * 2 * Q);
+        const int s = rem / Q, j = rem - s * Q;
+        const long t = a.t0 + tl;
+        const int ii = inst_of(a.mc, a.n_inst, t);
+        const InstMC& I = a.mc[ii];
+        const GridInst& G = a.gi[ii];
+        const float2 x = a.pos[t];
+        // counter = (sample | sign, instance-local target, step): an ensemble
+        // member draws exactly what a standalone run with its seed draws
+        const U4 r = philox4x32_10(U4{uint32_t(j) | (uint32_t(s) << 31), uint32_t(t - I.p_begin), uint32_t(step),
+                                      uint32_t(step >> 32)},
+                                   I.key0, I.key1);
+        float2 y = x;
+        bool valid = true;
+        if (j < a.N1) {
+            const int n = I.cnt[s];
+            if (n == 0) {
+                valid = false;
+            } else {
+                const int idx = sample_cdf(a.cdf + I.off[s], a.guide + I.goff[s], n, u01d(r.x));
+                const int p = a.sub[I.off[s] + idx] + I.p_begin;   // subsets hold instance-local indices
+                y = a.pos[p];
+                if (I.periodic) {
+                    const int m9 = min(int(u01(r.y) * 9.f), 8);
+                    y.x += float(m9 / 3 - 1) * I.Lx;
+                    y.y += float(m9 % 3 - 1) * I.Ly;
+                }
+                float rr;
+                const float ur = u01(r.z);
+                if (I.law == VPMC_LAW_REFERENCE) {
+                    // sample_kernel_radius (include/monte_carlo_bs.cuh:78-88): the
+                    // table already holds h_w and is scaled by h_w once more
+                    const float f = ur * (kIcdfRef - 1);
+                    const int i0 = int(f), i1 = min(i0 + 1, kIcdfRef - 1);
+                    const float tt = f - i0;
+                    rr = (I.icdf[i0] * (1.f - tt) + I.icdf[i1] * tt) * I.hw;
+                } else {
+                    const float f = ur * kJitTab;
+                    const int i0 = min(int(f), kJitTab - 1);
+                    const float tt = f - i0;
+                    rr = (a.jit[i0] * (1.f - tt) + a.jit[i0 + 1] * tt) * I.hw;
+                }
+                float sn, cs;
+                sincosf(2.f * kPiF * u01(r.w), &sn, &cs);
+                y.x += rr * cs;
+                y.y += rr * sn;
+            }
+        } else {
+            const float R = disk_radius(x, I.periodic != 0, I.Lx, I.Ly);
+            const float phi = 2.f * kPiF * u01(r.x);
+            const float ur = u01(r.y);
+            const float rr = I.law == VPMC_LAW_REFERENCE ? R * sqrtf(ur) : R * ur;
+            float sn, cs;
+            sincosf(phi, &sn, &cs);
+            y.x = x.x + rr * cs;
+            y.y = x.y + rr * sn;
+        }
+        uint32_t b = kNoBin;
+        if (valid) {
+            float px = y.x, py = y.y;
+            bool ok = true;
+            if (I.periodic) {
+                const float kx = floorf(px / I.Lx), ky = floorf(py / I.Ly);
+                if (I.law == VPMC_LAW_UNBIASED && (fabsf(kx) > 2.f || fabsf(ky) > 2.f)) ok = false;
+                px -= kx * I.Lx;
+                py -= ky * I.Ly;
+            } else {
+                ok = !(px < 0.f || px > I.Lx || py < 0.f || py > I.Ly);
+            }
+            if (ok) {
+                const int cx = min(max(floor_int(px * G.inv_sx), 0), G.gx - 1);
+                const int cy = min(max(floor_int(py * G.inv_sy), 0), G.gy - 1);
+                b = uint32_t(G.bin_base) + uint32_t(s) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
+                atomicAdd(&a.qcount[b], 1u);
+            }
+        }
+        a.ys[sid] = y;
+        a.qbin[sid] = b;
+    }
+}
+
+struct AccArgs {
+    const InstMC* mc;
+    int n_inst;
+    const float2* pos;
+    const float2* ys;
+    const float* fv;       // field value per sample
+    long t0, nt;
+    int N1, N2;
+    int advect;
+    float2* vel;
+    float2* pos_out;
+};
+
+// mis_contrib_dev (src/cuda/monte_carlo_bs.cu:35-51) for the reference law;
+// the balance-heuristic estimator with the true sampling densities for the
+// unbiased law.
+__device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f, float w1, float w2, float cum,
+                                           float alpha, float R, const InstMC& I) {
+    if (!(f > 0.f)) return make_float2(0.f, 0.f);
+    const float rx = x.x - y.x, ry = x.y - y.y;
+    if (law == VPMC_LAW_REFERENCE) {
+        float wx = rx, wy = ry;
+        if (I.periodic) {
+            wx = rx - roundf(rx / I.Lx) * I.Lx;
+            wy = ry - roundf(ry / I.Ly) * I.Ly;
+        }
+        const float rn = fmaxf(sqrtf(wx * wx + wy * wy), 1e-6f);
+        const float inv_r2 = 1.f / (rx * rx + ry * ry + 1e-8f);
+        const float kx = -ry * inv_r2 / (2 * kPiF), ky = rx * inv_r2 / (2 * kPiF);
+        const float denom = w1 * f / cum + w2 * alpha / rn;
+        const float sc = f / denom;
+        return make_float2(kx * sc, ky * sc);
+    }
+    const float r2 = rx * rx + ry * ry;
+    if (!(r2 > 0.f)) return make_float2(0.f, 0.f);
+    const float rn = sqrtf(r2);
+    const float p2 = rn < R ? alpha / rn : 0.f;
+    const float denom = w1 * f / cum + w2 * p2;
+    const float sc = f / (denom * (2.f * kPiF * r2));
+    return make_float2(-ry * sc, rx * sc);
+}
+
+__global__ void __launch_bounds__(256) k_accum(AccArgs a) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
+    const int Q = a.N1 + a.N2;
+    const float w1 = float(a.N1) / float(Q), w2 = float(a.N2) / float(Q);
+    const float inv = 1.f / float(Q);
+    for (long tl = warp; tl < a.nt; tl += nwarps) {
+        const long t = a.t0 + tl;
+        const InstMC& I = a.mc[inst_of(a.mc, a.n_inst, t)];
+        const float2 x = a.pos[t];
+        const float R = disk_radius(x, I.periodic != 0, I.Lx, I.Ly);
+        const float alpha = 1.f / (2.f * kPiF * R);
+        float u[2][2];
+        for (int s = 0; s < 2; ++s) {
+            KSum sx, sy;
+            const long base = (tl * 2 + s) * Q;
+            for (int j = lane; j < Q; j += 32) {
+                const float2 y = a.ys[base + j];
+                const float f = a.fv[base + j];
+                const float2 c = mis_term(I.law, x, y, f, w1, w2, I.cum9[s], alpha, R, I);
+                sx.add(c.x);
+                sy.add(c.y);
+            }
+            u[s][0] = warp_sum_comp(sx.s, sx.c) * inv;
+            u[s][1] = warp_sum_comp(sy.s, sy.c) * inv;
+        }
+        if (lane == 0) {
+            const float vx = u[0][0] - u[1][0], vy = u[0][1] - u[1][1];
+            a.vel[t] = make_float2(vx, vy);
+            if (a.advect) {
+                double nx = double(x.x) + double(I.dt) * double(vx);
+                double ny = double(x.y) + double(I.dt) * double(vy);
+                float ox, oy;
+                if (I.periodic) {
+                    nx -= floor(nx / double(I.Lx)) * double(I.Lx);
+                    ny -= floor(ny / double(I.Ly)) * double(I.Ly);
+                    ox = float(nx);
+                    oy = float(ny);
+                    if (ox >= I.Lx) ox = 0.f;
+                    if (oy >= I.Ly) oy = 0.f;
+                } else {
+                    ox = float(nx);
+                    oy = float(ny);
+                }
+                a.pos_out[t] = make_float2(ox, oy);
+            }
+        }
+    }
+}
+
+__global__ void k_inc_step(unsigned long long* s) { *s += 1ull; }
+
+__global__ void k_taylor_green(const float2* __restrict__ pos, long n, float* __restrict__ b) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const double x = pos[i].x, y = pos[i].y;
+        b[i] = float(4.0 * kPiD * sin(2.0 * kPiD * x) * sin(2.0 * kPiD * y));
+    }
+}
+
+__global__ void k_check_finite(const float2* __restrict__ p, long n, unsigned* flags) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const float2 v = p[i];
+        if (!isfinite(v.x) || !isfinite(v.y)) atomicOr(flags, FLAG_NONFINITE);
+    }
+}
+
+int blocks_for(long n, int threads = 256) {
+    long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 65535L * 16) b = 65535L * 16;
+    return int(b);
+}
+
+// Inverse of the radial mass C(q) of the cubic spline (2 pi r W(r) dr, h_w = 1)
+// tabulated at u = i / T by bisection in FP64; the unbiased branch-1 jitter
+// radius is h_w * interp(u).
+void build_jitter_table(std::vector<float>& t) {
+    t.resize(kJitTab + 1);
+    for (int i = 0; i <= kJitTab; ++i) {
+        const double u = double(i) / kJitTab;
+        double lo = 0.0, hi = 1.0;
+        for (int it = 0; it < 80; ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (spline_mass_d(mid) < u) lo = mid; else hi = mid;
+        }
+        t[i] = float(0.5 * (lo + hi));
+    }
+    t[0] = 0.f;
+    t[kJitTab] = 1.f;
+}
+
+}  // namespace
+}  // namespace vpmc
+
+using namespace vpmc;
+
+struct vpmc_sim {
+    vpmc_context* ctx = nullptr;
+    int n_inst = 0;
+    std::vector<vpmc_sim_params> prm;
+    std::vector<int> counts;
+    std::vector<long> begin;
+    long N = 0;
+    int N1 = 0, N2 = 0;
+    uint64_t step = 0;
+    int k_walk = 0, qpt = 4;
+    bool prepared = false;
+    // device state
+    DevBuf mem;                        // particles, subsets, tables
+    float2* pos = nullptr;
+    float2* pos_next = nullptr;
+    float2* vel = nullptr;
+    float* omega = nullptr;
+    int* sub = nullptr;                // instance i: positives at 2*b_i, negatives at 2*b_i + n_i
+    double* cdf = nullptr;
+    uint32_t* guide = nullptr;
+    float* jit = nullptr;
+    InstMC* d_mc = nullptr;
+    unsigned long long* d_step = nullptr;
+    std::vector<InstMC> mc;
+    // grid + sample working set
+    DevBuf work;
+    std::vector<GridInst> plan;
+    GridBufs g;
+    ItemBufs it;
+    QueryBufs q;
+    float2* ys = nullptr;
+    float* fv = nullptr;
+    long chunk_targets = 0;
+    long max_samples = 0;
+    // graphs
+    cudaGraphExec_t graph_step = nullptr;
+    cudaGraphExec_t graph_vel = nullptr;
+    int launches_per_step = 0;
+    float eval_ms = 0.f;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+void drop_graphs(vpmc_sim* s) {
+    if (s->graph_step) cudaGraphExecDestroy(s->graph_step);
+    if (s->graph_vel) cudaGraphExecDestroy(s->graph_vel);
+    s->graph_step = s->graph_vel = nullptr;
+}
+
+uint32_t mix32(uint64_t v) {
+    v ^= v >> 33;
+    v *= 0xff51afd7ed558ccdULL;
+    v ^= v >> 33;
+    v *= 0xc4ceb9fe1a85ec53ULL;
+    v ^= v >> 33;
+    return uint32_t(v);
+}
+
+// Philox key of an instance = its own 64-bit seed (scrambled so that small
+// seeds give unrelated keys); nothing else enters the key.
+void set_keys(vpmc_sim* s) {
+    for (int i = 0; i < s->n_inst; ++i) {
+        const uint64_t seed = s->prm[i].seed;
+        s->mc[i].key0 = mix32(seed * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL);
+        s->mc[i].key1 = mix32(seed ^ 0xA4093822299F31D0ULL);
+        s->mc[i].law = s->prm[i].law;
+    }
+}
+
+int upload_mc(vpmc_sim* s) {
+    VPMC_CUDA(cudaMemcpyAsync(s->d_mc, s->mc.data(), sizeof(InstMC) * s->mc.size(), cudaMemcpyHostToDevice,
+                              s->ctx->stream));
+    return VPMC_OK;
+}
+
+// Working set sized for the largest chunk (samples <= max_samples).
+int alloc_work(vpmc_sim* s) {
+    vpmc_context* ctx = s->ctx;
+    std::vector<InstDesc> d(s->n_inst);
+    for (int i = 0; i < s->n_inst; ++i)
+        d[i] = InstDesc{s->prm[i].Lx, s->prm[i].Ly, s->mc[i].hw, s->prm[i].periodic, int(s->begin[i]),
+                        int(s->begin[i] + s->counts[i])};
+    s->plan.resize(s->n_inst);
+    const long nb = grid_plan(d.data(), s->n_inst, s->k_walk, 2, s->plan.data());
+    if (nb < 0) return int(-nb);
+    const long Q2 = 2L * (s->N1 + s->N2);
+    long per_chunk = s->max_samples / Q2;
+    if (per_chunk < 1) per_chunk = 1;
+    if (per_chunk > s->N) per_chunk = s->N;
+    s->chunk_targets = per_chunk;
+    const long ns = per_chunk * Q2;
+    auto carve_all = [&](Carver& c) {
+        carve_grid(c, s->N, nb, s->n_inst, &s->g);
+        carve_items(c, nb, ns, &s->it);
+        carve_queries(c, nb, ns, &s->q);
+        s->ys = c.take<float2>(size_t(ns));
+        s->fv = c.take<float>(size_t(ns));
+    };
+    Carver dry;
+    carve_all(dry);
+    drop_graphs(s);
+    VPMC_TRY(s->work.reserve(dry.off));
+    Carver c{static_cast<char*>(s->work.p), 0};
+    carve_all(c);
+    VPMC_CUDA(cudaMemcpyAsync(s->g.inst, s->plan.data(), sizeof(GridInst) * s->plan.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    return VPMC_OK;
+}
+
+// Issue one MIS pass over all targets (advect: positions -> pos_next, then
+// copied back, step counter incremented).  No host synchronisation inside, so
+// it can be captured.  Returns launches issued.
+int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
+    vpmc_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const uint64_t l0 = vpmc_kernel_launch_count();
+    VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
+    const int Q = s->N1 + s->N2;
+    float ms_total = 0.f;
+    for (long t0 = 0; t0 < s->N; t0 += s->chunk_targets) {
+        const long nt = std::min(s->chunk_targets, s->N - t0);
+        const long ns = nt * 2 * Q;
+        VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
+        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
+                   nt, s->N1, s->N2, s->ys, s->q.qbin, s->q.qcount};
+        VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
+        VPMC_TRY(scatter_points(ctx, s->g, s->q, s->ys, ns, 0));
+        VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->qpt)));
+        VPMC_CUDA(cudaMemsetAsync(s->fv, 0, sizeof(float) * size_t(ns), st));
+        EvalLaunch L;
+        L.mode = s->mc[0].law == VPMC_LAW_UNBIASED ? EVAL_FIELD9 : EVAL_FIELD;
+        L.qpt = s->qpt;
+        L.out_f32 = s->fv;
+        if (timed) VPMC_CUDA(cudaEventRecord(s->ev[0], st));
+        VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
+        if (timed) {
+            VPMC_CUDA(cudaEventRecord(s->ev[1], st));
+            VPMC_CUDA(cudaEventSynchronize(s->ev[1]));
+            float ms = 0.f;
+            VPMC_CUDA(cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
+            ms_total += ms;
+        }
+        AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
+                   s->pos_next};
+        VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
+    }
+    if (advect) {
+        VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+        VPMC_LAUNCH(k_inc_step, 1, 1, 0, st, s->d_step);
+    }
+    if (timed) s->eval_ms = ms_total;
+    *nlaunch = int(vpmc_kernel_launch_count() - l0);
+    return VPMC_OK;
+}
+
+int run_pass(vpmc_sim* s, bool advect, int use_graph) {
+    vpmc_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
+    if (s->mc[0].law == VPMC_LAW_UNBIASED)
+        for (auto& m : s->mc) if (m.law != VPMC_LAW_UNBIASED) return VPMC_ERR_INVALID;
+    cudaGraphExec_t* gx = advect ? &s->graph_step : &s->graph_vel;
+    if (!use_graph) {
+        int nl = 0;
+        VPMC_TRY(issue_pass(s, advect, true, &nl));
+        s->launches_per_step = nl;
+        if (advect) s->step += 1;
+        return VPMC_OK;
+    }
+    if (!*gx) {
+        // eager pass first (sets kernel attributes, sizes the eval grid), then capture
+        int nl = 0;
+        VPMC_TRY(issue_pass(s, advect, false, &nl));
+        VPMC_CUDA(cudaStreamSynchronize(st));
+        if (advect) s->step += 1;
+        cudaGraph_t graph = nullptr;
+        VPMC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = issue_pass(s, advect, false, &nl);
+        const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (rc != VPMC_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+        VPMC_CUDA(ce);
+        const cudaError_t ie = cudaGraphInstantiate(gx, graph, 0);
+        cudaGraphDestroy(graph);
+        VPMC_CUDA(ie);
+        s->launches_per_step = nl;
+        if (advect) return VPMC_OK;   // the eager pass was this call's step
+    }
+    VPMC_CUDA(cudaGraphLaunch(*gx, st));
+    if (advect) s->step += 1;
+    return VPMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, const int* counts, vpmc_sim** out) {
+    if (!ctx || n_inst < 1 || !prms || !counts || !out) return VPMC_ERR_INVALID;
+    *out = nullptr;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    long N = 0;
+    for (int i = 0; i < n_inst; ++i) {
+        const vpmc_sim_params& p = prms[i];
+        if (counts[i] < 0 || p.Nx < 1 || !(p.hwr > 0.f) || !(p.Lx > 0.f) || !(p.Ly > 0.f)) return VPMC_ERR_INVALID;
+        if (p.N1 < 0 || p.N2 < 0 || p.N1 + p.N2 < 1 || p.N1 != prms[0].N1 || p.N2 != prms[0].N2) return VPMC_ERR_INVALID;
+        if (p.law != VPMC_LAW_REFERENCE && p.law != VPMC_LAW_UNBIASED) return VPMC_ERR_INVALID;
+        if (p.law != prms[0].law) return VPMC_ERR_INVALID;
+        N += counts[i];
+    }
+    if (N >= (1L << 31) || N < 1) return N < 1 ? VPMC_ERR_INVALID : VPMC_ERR_CAPACITY;
+    auto* s = new (std::nothrow) vpmc_sim();
+    if (!s) return VPMC_ERR_NOMEM;
+    s->ctx = ctx;
+    s->n_inst = n_inst;
+    s->prm.assign(prms, prms + n_inst);
+    s->counts.assign(counts, counts + n_inst);
+    s->begin.resize(n_inst);
+    s->N = N;
+    s->N1 = prms[0].N1;
+    s->N2 = prms[0].N2;
+    s->max_samples = 1L << 27;
+    long b = 0;
+    s->mc.resize(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+        s->begin[i] = b;
+        const vpmc_sim_params& p = prms[i];
+        InstMC m{};
+        // SimParam (include/vortex_particle_mc.hpp:119-133): h = Lx/Nx, h_w = h*hwr
+        const float h = p.Lx / float(p.Nx);
+        m.hw = h * p.hwr;
+        m.Lx = p.Lx;
+        m.Ly = p.Ly;
+        m.dt = p.dt;
+        m.periodic = p.periodic;
+        m.law = p.law;
+        m.p_begin = int(b);
+        m.p_end = int(b + counts[i]);
+        float cdf[kIcdfRef];
+        vpmc_kernel_icdf_table(m.hw, kIcdfRef, cdf, m.icdf);
+        s->mc[i] = m;
+        b += counts[i];
+    }
+    set_keys(s);
+    // particle + subset memory
+    Carver dry;
+    auto carve_state = [&](Carver& c) {
+        s->pos = c.take<float2>(size_t(N));
+        s->pos_next = c.take<float2>(size_t(N));
+        s->vel = c.take<float2>(size_t(N));
+        s->omega = c.take<float>(size_t(N));
+        s->sub = c.take<int>(2 * size_t(N) + 2);
+        s->cdf = c.take<double>(2 * size_t(N) + 2);
+        s->guide = c.take<uint32_t>(size_t(N) + 4 * size_t(n_inst) + 4);
+        s->jit = c.take<float>(kJitTab + 2);
+        s->d_mc = c.take<InstMC>(size_t(n_inst));
+        s->d_step = c.take<unsigned long long>(1);
+    };
+    carve_state(dry);
+    int rc = s->mem.reserve(dry.off);
+    if (rc != VPMC_OK) { delete s; return rc; }
+    Carver c{static_cast<char*>(s->mem.p), 0};
+    carve_state(c);
+    std::vector<float> jt;
+    build_jitter_table(jt);
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(s->mem.p, 0, s->mem.bytes, st);
+    cudaMemcpyAsync(s->jit, jt.data(), sizeof(float) * jt.size(), cudaMemcpyHostToDevice, st);
+    unsigned long long zero = 0;
+    cudaMemcpyAsync(s->d_step, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+    if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess) {
+        vpmc_sim_destroy(s);
+        return VPMC_ERR_CUDA;
+    }
+    rc = upload_mc(s);
+    if (rc == VPMC_OK) rc = alloc_work(s);
+    if (rc == VPMC_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = VPMC_ERR_CUDA;
+    if (rc != VPMC_OK) { vpmc_sim_destroy(s); return rc; }
+    *out = s;
+    return VPMC_OK;
+}
+
+int vpmc_sim_destroy(vpmc_sim* s) {
+    if (!s) return VPMC_ERR_INVALID;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    drop_graphs(s);
+    for (auto& e : s->ev) if (e) cudaEventDestroy(e);
+    s->mem.release();
+    s->work.release();
+    delete s;
+    return VPMC_OK;
+}
+
+int vpmc_sim_num_particles(vpmc_sim* s) { return s ? int(s->N) : -1; }
+
+int vpmc_sim_set_particles(vpmc_sim* s, const float* pos, const float* omega, int is_host) {
+    if (!s) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    const cudaMemcpyKind k = is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (pos) {
+        VPMC_CUDA(cudaMemcpyAsync(s->pos, pos, sizeof(float2) * size_t(s->N), k, st));
+        VPMC_LAUNCH(k_check_finite, blocks_for(s->N), 256, 0, st, s->pos, s->N, s->ctx->d_flags);
+    }
+    if (omega) {
+        VPMC_CUDA(cudaMemcpyAsync(s->omega, omega, sizeof(float) * size_t(s->N), k, st));
+        s->prepared = false;
+    }
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_get_particles(vpmc_sim* s, float* pos, float* omega, float* vel, int is_host) {
+    if (!s) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    const cudaMemcpyKind k = is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (pos) VPMC_CUDA(cudaMemcpyAsync(pos, s->pos, sizeof(float2) * size_t(s->N), k, st));
+    if (omega) VPMC_CUDA(cudaMemcpyAsync(omega, s->omega, sizeof(float) * size_t(s->N), k, st));
+    if (vel) VPMC_CUDA(cudaMemcpyAsync(vel, s->vel, sizeof(float2) * size_t(s->N), k, st));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_prepare(vpmc_sim* s) {
+    if (!s) return VPMC_ERR_INVALID;
+    vpmc_context* ctx = s->ctx;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    long goff = 0;
+    for (int i = 0; i < s->n_inst; ++i) {
+        const long b = s->begin[i], n = s->counts[i];
+        InstMC& m = s->mc[i];
+        int cnt[2] = {0, 0};
+        double cum[2] = {0, 0};
+        if (n > 0)
+            VPMC_TRY(build_subsets_dev(ctx, n, s->omega + b, s->sub + 2 * b, s->sub + 2 * b + n, s->cdf + 2 * b,
+                                       s->cdf + 2 * b + n, nullptr, nullptr, cnt, cum));
+        m.cnt[0] = cnt[0];
+        m.cnt[1] = cnt[1];
+        m.off[0] = 2 * b;
+        m.off[1] = 2 * b + n;
+        const float f9 = m.periodic ? 9.f : 1.f;
+        m.cum9[0] = float(cum[0]) * f9;
+        m.cum9[1] = float(cum[1]) * f9;
+        for (int sg = 0; sg < 2; ++sg) {
+            m.goff[sg] = goff;
+            if (cnt[sg] > 0)
+                VPMC_LAUNCH(k_guide, blocks_for(cnt[sg] + 1), 256, 0, st, s->cdf + m.off[sg], cnt[sg], s->guide + goff);
+            goff += cnt[sg] + 2;
+        }
+    }
+    VPMC_TRY(upload_mc(s));
+    VPMC_CUDA(cudaStreamSynchronize(st));
+    drop_graphs(s);
+    s->prepared = true;
+    return vpmc_context_sync(ctx);
+}
+
+int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, int max_iter, double* info) {
+    if (!s) return VPMC_ERR_INVALID;
+    vpmc_context* ctx = s->ctx;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    float* b = nullptr;
+    if (!omega_field) {
+        b = s->fv;   // reuse sample-value scratch for the right-hand side (>= N floats)
+        if (s->max_samples < s->N) return VPMC_ERR_CAPACITY;
+        VPMC_LAUNCH(k_taylor_green, blocks_for(s->N), 256, 0, st, s->pos, s->N, b);
+    }
+    int worst = VPMC_OK;
+    for (int i = 0; i < s->n_inst; ++i) {
+        const long off = s->begin[i];
+        const vpmc_sim_params& p = s->prm[i];
+        double inf[3] = {0, 0, 0};
+        const float* bi = omega_field ? omega_field + off : b + off;
+        const int rc = vpmc_cg_rbf(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off), bi,
+                                   s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol, max_iter, inf);
+        if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) return rc;
+        if (rc != VPMC_OK) worst = rc;
+        if (info) { info[3 * i] = inf[0]; info[3 * i + 1] = inf[1]; info[3 * i + 2] = inf[2]; }
+    }
+    s->prepared = false;
+    VPMC_TRY(vpmc_sim_prepare(s));
+    return worst;
+}
+
+int vpmc_sim_step(vpmc_sim* s, int nsteps, int use_graph) {
+    if (!s || nsteps < 0) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    for (int k = 0; k < nsteps; ++k) VPMC_TRY(run_pass(s, true, use_graph));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_velocity(vpmc_sim* s, uint64_t step, float* vel) {
+    if (!s || !vel) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    unsigned long long v = step;
+    VPMC_CUDA(cudaMemcpyAsync(s->d_step, &v, sizeof(v), cudaMemcpyHostToDevice, st));
+    VPMC_TRY(run_pass(s, false, 0));
+    VPMC_CUDA(cudaMemcpyAsync(vel, s->vel, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+    unsigned long long cur = s->step;
+    VPMC_CUDA(cudaMemcpyAsync(s->d_step, &cur, sizeof(cur), cudaMemcpyHostToDevice, st));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_step_host(vpmc_sim* s, const float* pos_in, float* pos_out, float* vel_out) {
+    if (!s) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    if (pos_in) VPMC_CUDA(cudaMemcpyAsync(s->pos, pos_in, sizeof(float2) * size_t(s->N), cudaMemcpyHostToDevice, st));
+    VPMC_TRY(run_pass(s, true, 1));
+    if (pos_out) VPMC_CUDA(cudaMemcpyAsync(pos_out, s->pos, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToHost, st));
+    if (vel_out) VPMC_CUDA(cudaMemcpyAsync(vel_out, s->vel, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToHost, st));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_set_law(vpmc_sim* s, int law) {
+    if (!s || (law != VPMC_LAW_REFERENCE && law != VPMC_LAW_UNBIASED)) return VPMC_ERR_INVALID;
+    for (auto& p : s->prm) p.law = law;
+    set_keys(s);
+    VPMC_TRY(upload_mc(s));
+    drop_graphs(s);
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_set_seed(vpmc_sim* s, uint64_t seed) {
+    if (!s) return VPMC_ERR_INVALID;
+    for (auto& p : s->prm) p.seed = seed;
+    set_keys(s);
+    VPMC_TRY(upload_mc(s));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_set_step(vpmc_sim* s, uint64_t step) {
+    if (!s) return VPMC_ERR_INVALID;
+    s->step = step;
+    unsigned long long v = step;
+    VPMC_CUDA(cudaMemcpyAsync(s->d_step, &v, sizeof(v), cudaMemcpyHostToDevice, s->ctx->stream));
+    return vpmc_context_sync(s->ctx);
+}
+
+uint64_t vpmc_sim_get_step(vpmc_sim* s) { return s ? s->step : 0; }
+
+int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
+    if (!s || k_walk < 0 || k_walk > 4 || !(qpt == 0 || qpt == 1 || qpt == 2 || qpt == 4)) return VPMC_ERR_INVALID;
+    s->k_walk = k_walk;
+    s->qpt = qpt == 0 ? 4 : qpt;
+    VPMC_TRY(alloc_work(s));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_get_tuning(vpmc_sim* s, int* k_walk, int* qpt) {
+    if (!s) return VPMC_ERR_INVALID;
+    if (k_walk) *k_walk = s->plan.empty() ? 0 : s->plan[0].k;
+    if (qpt) *qpt = s->qpt;
+    return VPMC_OK;
+}
+
+int vpmc_sim_last_stats(vpmc_sim* s, int* launches_per_step, float* eval_ms) {
+    if (!s) return VPMC_ERR_INVALID;
+    if (launches_per_step) *launches_per_step = s->launches_per_step;
+    if (eval_ms) *eval_ms = s->eval_ms;
+    return VPMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,378 @@
+"""phash -- Python binding of the GB300 hot path (mirror of the reference's
+`phash` pybind11 module, bindings/phash.cpp:6-14, which only exposed
+``fill_dummy()``).  Every function here calls libvpmc.so through its C ABI on
+CUDA tensors; there is no CPU path.
+
+Tensors: positions are (N, 2) float32, strengths (N,) float32, index arrays
+int32, all on the same CUDA device.  Each call runs on torch's current stream
+of that device (the library context borrows it), so results are ordered with
+surrounding torch work.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, SimParams, check, lib)
+
+__all__ = [
+    "fill_dummy", "Context", "context", "fill_cells", "counting_sort", "hash_build", "build_subsets",
+    "kernel_icdf_table", "cubic_spline", "query_vorticity", "rbf_matvec", "cg_rbf", "direct_velocity",
+    "Simulation", "SimParam", "philox4x32_10", "launch_count", "LAW_REFERENCE", "LAW_UNBIASED",
+    "DIRECT_MOLLIFIED", "DIRECT_PLUMMER",
+]
+
+
+def fill_dummy() -> str:
+    """Smoke entry point kept from the reference binding (bindings/phash.cpp:10-13)."""
+    lib()  # the native library must be loadable
+    return "phash imported OK"
+
+
+class Context:
+    """vpmc_context bound to a device and a stream (torch's current stream
+    when not given)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("phash needs a CUDA device (no CPU fallback)")
+        self.device = device
+        if stream is None:
+            stream = torch.cuda.current_stream(device).cuda_stream
+        self.stream = stream
+        h = C.c_void_p()
+        check(lib().vpmc_context_create(device, C.c_void_p(stream), C.byref(h)), "vpmc_context_create")
+        self.h = h
+
+    def sync(self):
+        check(lib().vpmc_context_sync(self.h), "vpmc_context_sync")
+
+    def scratch_bytes(self) -> int:
+        return int(lib().vpmc_context_scratch_bytes(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vpmc_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+_CTX: dict = {}
+
+
+def context(device: int | None = None) -> Context:
+    """Default context of `device` on torch's current stream."""
+    if device is None:
+        device = torch.cuda.current_device()
+    stream = torch.cuda.current_stream(device).cuda_stream
+    key = (device, stream)
+    if key not in _CTX:
+        _CTX[key] = Context(device, stream)
+    return _CTX[key]
+
+
+def _p(t):
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _cuda(t, dtype, name, shape=None):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}")
+    if shape is not None and tuple(t.shape[1:]) != shape:
+        raise ValueError(f"{name} must have trailing shape {shape}")
+    return t.contiguous()
+
+
+def _dev(t):
+    return t.device.index if t.device.index is not None else torch.cuda.current_device()
+
+
+# ---------------------------------------------------------------- hash (a1-a3)
+def fill_cells(rshx, rshy, Lx, Ly, pos, sub=None):
+    """FillCells_cuda (src/cuda/hash.cu:42-69): returns (cell_num, cell_acc, vp_cell)."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    n = pos.shape[0] if sub is None else sub.shape[0]
+    if sub is not None:
+        sub = _cuda(sub, torch.int32, "sub")
+    dev = pos.device
+    cn = torch.empty(rshx * rshy, dtype=torch.int32, device=dev)
+    ca = torch.empty_like(cn)
+    vc = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    check(lib().vpmc_fill_cells(context(_dev(pos)).h, rshx, rshy, Lx, Ly, n, _p(sub), _p(pos), _p(cn), _p(ca),
+                                _p(vc)), "vpmc_fill_cells")
+    return cn, ca, vc[:n]
+
+
+def counting_sort(cell_num, cell_acc, vp_cell, ncell=None):
+    """CountingSort_cuda (src/cuda/hash.cu:71-91): returns vp_sort; cell_num is zeroed."""
+    vp_cell = _cuda(vp_cell, torch.int32, "vp_cell")
+    n = vp_cell.shape[0]
+    vs = torch.empty(max(n, 1), dtype=torch.int32, device=vp_cell.device)
+    nc = cell_num.shape[0] if ncell is None else ncell
+    check(lib().vpmc_counting_sort(context(_dev(vp_cell)).h, n, nc, _p(cell_num), _p(cell_acc), _p(vp_cell), _p(vs)),
+          "vpmc_counting_sort")
+    return vs[:n]
+
+
+def hash_build(rshx, rshy, Lx, Ly, pos, sub=None):
+    """FillCells + CountingSort: dict(cell_num, cell_acc, vp_cell, vp_sort)."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    n = pos.shape[0] if sub is None else sub.shape[0]
+    if sub is not None:
+        sub = _cuda(sub, torch.int32, "sub")
+    dev = pos.device
+    cn = torch.empty(rshx * rshy, dtype=torch.int32, device=dev)
+    ca = torch.empty_like(cn)
+    vc = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    vs = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    check(lib().vpmc_hash_build(context(_dev(pos)).h, rshx, rshy, Lx, Ly, n, _p(sub), _p(pos), _p(cn), _p(ca),
+                                _p(vc), _p(vs)), "vpmc_hash_build")
+    return dict(cell_num=cn, cell_acc=ca, vp_cell=vc[:n], vp_sort=vs[:n])
+
+
+# ---------------------------------------------------------------- subsets (a4)
+def build_subsets(omega):
+    """build_subsets_cuda (src/cuda/build_particle_sets.cu:11-89) with FP64 CDFs."""
+    omega = _cuda(omega, torch.float32, "omega")
+    n = omega.shape[0]
+    dev = omega.device
+    sp = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    sn = torch.empty_like(sp)
+    cp = torch.empty(max(n, 1), dtype=torch.float64, device=dev)
+    cn = torch.empty_like(cp)
+    c32p = torch.empty(max(n, 1), dtype=torch.float32, device=dev)
+    c32n = torch.empty_like(c32p)
+    cnt = (C.c_int * 2)()
+    cum = (C.c_double * 2)()
+    check(lib().vpmc_build_subsets(context(_dev(omega)).h, n, _p(omega), _p(sp), _p(sn), _p(cp), _p(cn), _p(c32p),
+                                   _p(c32n), C.cast(cnt, C.c_void_p), C.cast(cum, C.c_void_p)), "vpmc_build_subsets")
+    a, b = cnt[0], cnt[1]
+    return dict(sub_pos=sp[:a], sub_neg=sn[:b], cdf_pos=cp[:a], cdf_neg=cn[:b], cdf32_pos=c32p[:a],
+                cdf32_neg=c32n[:b], cnt_pos=a, cnt_neg=b, cum_pos=cum[0], cum_neg=cum[1])
+
+
+def kernel_icdf_table(h_w: float, length: int = 20):
+    """build_cubic_rcdf + cdf_to_icdf (src/utilities.cu:12-96) -> (cdf, icdf) numpy float32."""
+    cdf = np.zeros(length, np.float32)
+    icdf = np.zeros(length, np.float32)
+    check(lib().vpmc_kernel_icdf_table(h_w, length, cdf.ctypes.data_as(C.c_void_p),
+                                       icdf.ctypes.data_as(C.c_void_p)), "vpmc_kernel_icdf_table")
+    return cdf, icdf
+
+
+def cubic_spline(r: float, h_w: float) -> float:
+    return float(lib().vpmc_cubic_spline(r, h_w))
+
+
+# ---------------------------------------------------------- vorticity query (a7)
+def query_vorticity(pos, omega, pts, sign=1, use_signed=False, exclude_center=False, h_w=0.04, Lx=1.0, Ly=1.0,
+                    periodic=True, F=None):
+    """queryVorticityAbs (include/vorticity_query.cuh:15-79) at every point of pts."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    omega = _cuda(omega, torch.float32, "omega")
+    pts = _cuda(pts, torch.float32, "pts", (2,))
+    out = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
+    check(lib().vpmc_query_vorticity(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(omega), _p(F), pts.shape[0],
+                                     _p(pts), int(sign), int(use_signed), int(exclude_center), h_w, Lx, Ly,
+                                     int(periodic), _p(out)), "vpmc_query_vorticity")
+    return out
+
+
+# ---------------------------------------------------------------- RBF / CG (a10)
+def rbf_matvec(pos, x, h_w, Lx=1.0, Ly=1.0, periodic=True, precise=True):
+    """Ax_cuda (src/cuda/cg_rbf_init.cu:33-50)."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    x = _cuda(x, torch.float32, "x")
+    y = torch.empty_like(x)
+    check(lib().vpmc_rbf_matvec(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(x), _p(y), h_w, Lx, Ly,
+                                int(periodic), int(precise)), "vpmc_rbf_matvec")
+    return y
+
+
+def cg_rbf(pos, b, h_w, Lx=1.0, Ly=1.0, periodic=True, tol=5e-3, max_iter=1000, allow_unconverged=False):
+    """conjugate_gradient_rbf (src/cuda/cg_rbf_init.cu:53-116) -> (omega, info dict)."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    b = _cuda(b, torch.float32, "b")
+    out = torch.empty_like(b)
+    info = (C.c_double * 3)()
+    st = lib().vpmc_cg_rbf(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(b), _p(out), h_w, Lx, Ly, int(periodic),
+                           tol, max_iter, C.cast(info, C.c_void_p))
+    if not (allow_unconverged and st == 9):
+        check(st, "vpmc_cg_rbf")
+    return out, dict(iters=int(info[0]), relres=info[1], true_relres=info[2], converged=st == 0)
+
+
+# ------------------------------------------------------------ direct sums (a11)
+def direct_velocity(pos, omega, kernel=DIRECT_MOLLIFIED, pts=None, tidx=None, param=0.04, Lx=1.0, Ly=1.0,
+                    periodic=True):
+    """FP64 direct Biot-Savart sums (src/cuda/naive_biot_savart.cu:15-40) -> (M, 2) float64."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    omega = _cuda(omega, torch.float32, "omega")
+    if kernel == DIRECT_PLUMMER:
+        tidx = _cuda(tidx, torch.int32, "tidx")
+        m = tidx.shape[0]
+    else:
+        pts = _cuda(pts, torch.float32, "pts", (2,))
+        m = pts.shape[0]
+    out = torch.empty((m, 2), dtype=torch.float64, device=pos.device)
+    check(lib().vpmc_direct_velocity_f64(context(_dev(pos)).h, kernel, pos.shape[0], _p(pos), _p(omega), m,
+                                         _p(pts), _p(tidx), param, Lx, Ly, int(periodic), _p(out)),
+          "vpmc_direct_velocity_f64")
+    return out
+
+
+# -------------------------------------------------------- simulation (a8,a9,a12)
+@dataclass
+class SimParam:
+    """SimParam (include/vortex_particle_mc.hpp:96-134) + estimator settings."""
+    dt: float = 0.01
+    Lx: float = 1.0
+    Ly: float = 1.0
+    Nx: int = 200
+    hwr: float = 16.0
+    N1: int = 1000
+    N2: int = 1000
+    periodic: bool = True
+    law: int = LAW_UNBIASED
+    seed: int = 0
+
+    def c(self) -> SimParams:
+        return SimParams(self.dt, self.Lx, self.Ly, self.Nx, self.hwr, self.N1, self.N2, int(self.periodic),
+                         int(self.law), int(self.seed))
+
+    @property
+    def h(self) -> float:
+        return float(np.float32(self.Lx) / np.float32(self.Nx))
+
+    @property
+    def h_w(self) -> float:
+        return float(np.float32(self.h) * np.float32(self.hwr))
+
+
+class Simulation:
+    """Simulation (include/vortex_particle_mc.hpp:136-192) over one or more
+    independent instances (an ensemble), each with its own SimParam."""
+
+    def __init__(self, params, counts, device: int | None = None):
+        if isinstance(params, SimParam):
+            params = [params]
+        counts = list(counts)
+        if len(counts) != len(params):
+            raise ValueError("one particle count per instance")
+        self.params = list(params)
+        self.counts = counts
+        self.ctx = context(device)
+        arr = (SimParams * len(params))(*[p.c() for p in params])
+        cnt = (C.c_int * len(counts))(*counts)
+        h = C.c_void_p()
+        check(lib().vpmc_sim_create(self.ctx.h, len(params), C.cast(arr, C.c_void_p), C.cast(cnt, C.c_void_p),
+                                    C.byref(h)), "vpmc_sim_create")
+        self.h = h
+        self.N = int(sum(counts))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vpmc_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def set_particles(self, pos, omega=None):
+        pos = _cuda(pos, torch.float32, "pos", (2,))
+        if omega is not None:
+            omega = _cuda(omega, torch.float32, "omega")
+        check(lib().vpmc_sim_set_particles(self.h, _p(pos), _p(omega), 0), "vpmc_sim_set_particles")
+
+    def set_particles_host(self, pos: np.ndarray, omega: np.ndarray | None = None):
+        pos = np.ascontiguousarray(pos, np.float32)
+        om = None if omega is None else np.ascontiguousarray(omega, np.float32)
+        check(lib().vpmc_sim_set_particles(self.h, pos.ctypes.data_as(C.c_void_p),
+                                           None if om is None else om.ctypes.data_as(C.c_void_p), 1),
+              "vpmc_sim_set_particles")
+
+    def particles(self):
+        dev = torch.device("cuda", self.ctx.device)
+        pos = torch.empty((self.N, 2), dtype=torch.float32, device=dev)
+        om = torch.empty(self.N, dtype=torch.float32, device=dev)
+        vel = torch.empty((self.N, 2), dtype=torch.float32, device=dev)
+        check(lib().vpmc_sim_get_particles(self.h, _p(pos), _p(om), _p(vel), 0), "vpmc_sim_get_particles")
+        return pos, om, vel
+
+    def init_strengths(self, omega_field=None, tol=1e-8, max_iter=1000, allow_unconverged=True):
+        info = (C.c_double * (3 * len(self.counts)))()
+        if omega_field is not None:
+            omega_field = _cuda(omega_field, torch.float32, "omega_field")
+        st = lib().vpmc_sim_init_strengths(self.h, _p(omega_field), tol, max_iter, C.cast(info, C.c_void_p))
+        if not (allow_unconverged and st == 9):
+            check(st, "vpmc_sim_init_strengths")
+        return [dict(iters=int(info[3 * i]), relres=info[3 * i + 1], true_relres=info[3 * i + 2])
+                for i in range(len(self.counts))]
+
+    def prepare(self):
+        check(lib().vpmc_sim_prepare(self.h), "vpmc_sim_prepare")
+
+    def step(self, nsteps: int = 1, use_graph: bool = True):
+        check(lib().vpmc_sim_step(self.h, nsteps, int(use_graph)), "vpmc_sim_step")
+
+    def step_host(self, pos_in: np.ndarray | None, pos_out: np.ndarray | None, vel_out: np.ndarray | None):
+        f = (lambda a: None if a is None else a.ctypes.data_as(C.c_void_p))
+        check(lib().vpmc_sim_step_host(self.h, f(pos_in), f(pos_out), f(vel_out)), "vpmc_sim_step_host")
+
+    def velocity(self, step: int = 0):
+        vel = torch.empty((self.N, 2), dtype=torch.float32, device=torch.device("cuda", self.ctx.device))
+        check(lib().vpmc_sim_velocity(self.h, int(step), _p(vel)), "vpmc_sim_velocity")
+        return vel
+
+    def set_law(self, law: int):
+        check(lib().vpmc_sim_set_law(self.h, int(law)), "vpmc_sim_set_law")
+
+    def set_seed(self, seed: int):
+        check(lib().vpmc_sim_set_seed(self.h, int(seed)), "vpmc_sim_set_seed")
+
+    def set_step(self, step: int):
+        check(lib().vpmc_sim_set_step(self.h, int(step)), "vpmc_sim_set_step")
+
+    @property
+    def step_count(self) -> int:
+        return int(lib().vpmc_sim_get_step(self.h))
+
+    def set_tuning(self, k_walk: int = 0, queries_per_thread: int = 0):
+        check(lib().vpmc_sim_set_tuning(self.h, int(k_walk), int(queries_per_thread)), "vpmc_sim_set_tuning")
+
+    def tuning(self):
+        k, q = C.c_int(), C.c_int()
+        check(lib().vpmc_sim_get_tuning(self.h, C.byref(k), C.byref(q)), "vpmc_sim_get_tuning")
+        return k.value, q.value
+
+    def last_stats(self):
+        n, ms = C.c_int(), C.c_float()
+        check(lib().vpmc_sim_last_stats(self.h, C.byref(n), C.byref(ms)), "vpmc_sim_last_stats")
+        return dict(launches_per_step=n.value, eval_ms=ms.value)
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 block (host evaluation, for known-answer tests)."""
+    c = (C.c_uint32 * 4)(*[int(v) & 0xffffffff for v in ctr])
+    k = (C.c_uint32 * 2)(*[int(v) & 0xffffffff for v in key])
+    o = (C.c_uint32 * 4)()
+    lib().vpmc_philox4x32_10(C.cast(c, C.c_void_p), C.cast(k, C.c_void_p), C.cast(o, C.c_void_p))
+    return [int(v) for v in o]
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(lib().vpmc_kernel_launch_count())
