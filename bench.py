@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark of the MIS Monte-Carlo Biot-Savart step (particle-steps/s).
+
+Default workload ``tg2048``: Taylor-Green vortex on a periodic unit square,
+cell-centred 2048^2 lattice (N = 4,194,304), hwr = 16 (h_w = 1/128),
+N1 = N2 = 64 samples per target and sign, dt = 2.5e-4, strengths from the
+CG-RBF solve (FP64 dots) of the Taylor-Green field.  Synthetic: no dataset.
+
+GPU arm (default): one step = hash rebuild + MIS velocity of every particle
+(both signs) + FP64-wrapped Euler advection, replayed as a CUDA graph.
+`value` = N * steps / device time with inputs resident; `e2e` = the same
+through the C-ABI host-buffer step (vpmc_sim_step_host: H2D positions, step,
+D2H positions + velocities per step).  The working set of a step (candidate
+array, 4.3 GB of sample records) is far larger than the 129 MB L2, so no L2
+flush is needed between steps.
+
+`--impl reference`: the reference's CPU estimator (monte_carlo_bs_cpu,
+restated bit-exactly in oracle/, OpenMP over targets on all host cores) on a
+bounded sample of targets of the same workload, one sample per step.
+
+Multi-GPU (torchrun): every rank runs its own replica of the workload (the
+path shards by independent instances; no collective), value = sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at fixed vel. RMS err vs FP64 direct sum; % HBM roofline"
+
+WORKLOADS = {
+    "tg2048": dict(Nx=2048, hwr=16.0, N1=64, N2=64, dt=2.5e-4),
+    "tg512": dict(Nx=512, hwr=16.0, N1=32, N2=32, dt=5e-4),
+    "tg256": dict(Nx=256, hwr=8.0, N1=32, N2=32, dt=1e-3),
+    "tg64": dict(Nx=64, hwr=4.0, N1=16, N2=16, dt=1e-3),
+}
+
+CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.th = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={CLOCK_QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.th:
+                self.th.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def profile_traffic(workload: str):
+    """DRAM bytes per eval launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"k_eval_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.lower().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_reference_sample(wl, pos, omega, budget_s, seed=17, nthreads=0, fixed_targets=None, st=None):
+    """Time the reference CPU estimator (oracle restatement of
+    monte_carlo_bs_cpu, pinned bit-exact to the reference sources) on a
+    bounded sample of targets.  Returns (particle-steps/s, threads, targets,
+    seconds, state); the subsets/hashes (state) are built once, outside the
+    timed part."""
+    import oracle as O
+    prm = O.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"])
+    if st is None:
+        st = O.OracleState(pos, omega, prm)
+    rng = np.random.default_rng(seed)
+    if fixed_targets is None:
+        t_probe = pos[rng.choice(len(pos), 16, replace=False)]
+        t0 = time.perf_counter()
+        _, nt = O.mc_velocity_omp(st, t_probe, prm.N1, prm.N2, seed, nthreads)
+        dt = time.perf_counter() - t0
+        m = int(np.clip(16 * budget_s / max(dt, 1e-6), 16, 200000))
+    else:
+        m = fixed_targets
+    targets = pos[rng.choice(len(pos), m, replace=m > len(pos))]
+    t0 = time.perf_counter()
+    vel, nt = O.mc_velocity_omp(st, targets, prm.N1, prm.N2, seed + 1, nthreads)
+    _ = targets + np.float32(prm.dt) * vel          # the Euler update of those targets
+    dt = time.perf_counter() - t0
+    return m / dt, nt, m, dt, st
+
+
+def strengths_cpu(wl, pos, b):
+    """One CG-RBF iteration on the CPU.  On the lattice the Taylor-Green field
+    b is an eigenvector of the RBF matrix A, so x0 = b / W(0) and the first CG
+    step lands on b / lambda; lambda is read off a few rows of A b (FP64)."""
+    import oracle as O
+    prm = O.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"])
+    st = O.OracleState(pos, b, prm)
+    rows = np.argsort(-np.abs(b))[:16]
+    Ab = O.query_vorticity_f64(st.view("all", w=b), pos[rows], 0, True, False, prm.h_w, True)
+    lam = float(np.median(Ab / b[rows].astype(np.float64)))
+    return (b.astype(np.float64) / lam).astype(np.float32), dict(iters=1, eigenvalue=lam)
+
+
+def run_reference(args, wl):
+    import oracle as O
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    pos = O.lattice(wl["Nx"])
+    b = O.taylor_green(pos)
+    # one CG iteration: on the lattice the Taylor-Green field is a single
+    # Fourier mode of the RBF matrix, so the first step already leaves only
+    # FP32 rounding of b; the timed estimator does not depend on the rest
+    omega, cg = strengths_cpu(wl, pos, b)
+    per_step_budget = max(1.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
+    rate, nt, m, dt, st = cpu_reference_sample(wl, pos, omega, per_step_budget)
+    times = []
+    for k in range(args.warmup + args.steps):
+        r, nt, _, d, _ = cpu_reference_sample(wl, pos, omega, 0, seed=100 + k, fixed_targets=m, st=st)
+        if k >= args.warmup:
+            times.append(d)
+    total = sum(times)
+    value = m * args.steps / total
+    out = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (Taylor-Green lattice)",
+        "impl": "reference",
+        "config": {"workload": args.workload, **wl, "N": len(pos), "law": "reference CPU (monte_carlo_bs_cpu)",
+                   "targets_per_step": m},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": nt, "kind": "port",
+                         "sample": f"{m} random targets of the {len(pos)}-particle workload per step, both signs, "
+                                   f"aux=0, Euler update; oracle/vpmc_oracle.cpp restating monte_carlo_bs_cpu"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cg": cg,
+    }
+    print(json.dumps(out))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU side
+def run_gpu(args, wl):
+    import torch
+    import torch.distributed as dist
+
+    import oracle as O
+    from vortexparticlemc_cuda_gb300 import phash as P
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    law = P.LAW_UNBIASED if args.law == "unbiased" else P.LAW_REFERENCE
+    pos = O.lattice(wl["Nx"])
+    N = len(pos)
+    sp = P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=rank)
+    sim = P.Simulation(sp, [N])
+    if args.k or args.qpt:
+        sim.set_tuning(args.k, args.qpt)
+    pos_d = torch.from_numpy(pos).to(dev)
+    sim.set_particles(pos_d, torch.zeros(N, device=dev))
+    t_cg = time.perf_counter()
+    cg = sim.init_strengths(None, tol=1e-8, max_iter=args.cg_iters)[0]
+    t_cg = time.perf_counter() - t_cg
+    _, omega_d, _ = sim.particles()
+
+    # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
+    # sum at 4096 random particles (seed 2)
+    err = None
+    if args.err_queries > 0:
+        idx = np.random.default_rng(2).choice(N, args.err_queries, replace=False)
+        v0 = sim.velocity(step=0)
+        q = pos_d[torch.from_numpy(idx).to(dev)]
+        truth = P.direct_velocity(pos_d, omega_d, P.DIRECT_MOLLIFIED, pts=q, param=sp.h_w).cpu().numpy()
+        est = v0[torch.from_numpy(idx).to(dev)].cpu().numpy().astype(np.float64)
+        rms = np.sqrt(np.mean(np.sum((est - truth) ** 2, 1)))
+        ref = np.sqrt(np.mean(np.sum(truth ** 2, 1)))
+        p = pos[idx].astype(np.float64)
+        tg = np.stack([np.sin(2 * np.pi * p[:, 0]) * np.cos(2 * np.pi * p[:, 1]),
+                       -np.cos(2 * np.pi * p[:, 0]) * np.sin(2 * np.pi * p[:, 1])], 1)
+        err = {"vel_rel_rms_vs_fp64_direct": rms / ref, "queries": int(args.err_queries),
+               "direct_vs_taylor_green_rel_rms": float(np.sqrt(np.mean(np.sum((truth - tg) ** 2, 1))) / ref)}
+
+    geo = sim.geometry()
+    sim.set_step(0)
+    sim.step(args.warmup, use_graph=True)
+    stream = torch.cuda.current_stream(dev)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    eval_ms = []
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            sim.step(1, use_graph=True)
+            eval_ms.append(sim.last_stats()["eval_ms"])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    stats = sim.last_stats()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * world * args.steps / (ms / 1e3)
+
+    # end to end through the host-buffer C-ABI call
+    pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
+    hp_in = pin(pos.copy())
+    hp_out = pin(np.zeros_like(pos))
+    hv_out = pin(np.zeros_like(pos))
+    a_in, a_out, a_vel = hp_in.numpy(), hp_out.numpy(), hv_out.numpy()
+    sim.step_host(a_in, a_out, a_vel)        # warm
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sim.step_host(a_in, a_out, a_vel)
+        a_in, a_out = a_out, a_in
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": N * world * args.e2e_steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": int(pos.nbytes), "d2h_bytes_per_step": int(2 * pos.nbytes),
+           "steps": args.e2e_steps, "call": "vpmc_sim_step_host (pinned host buffers)"}
+
+    # roofline of the dominant kernel (field evaluation, FP32-pipe bound)
+    peaks, peak_kind = measured_peaks()
+    Q = 2 * (wl["N1"] + wl["N2"])
+    n_hit = np.pi * wl["hwr"] ** 2 / 2.0            # same-sign particles within h_w (TG: half of them)
+    launches = max(1, geo["chunks"])
+    eval_ms_launch = float(np.mean(eval_ms)) / launches
+    samples_launch = N * Q / launches
+    flop_launch = samples_launch * n_hit * 16.0
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    achieved = flop_launch / (eval_ms_launch / 1e3) / 1e12
+    clocks = clk.summary()
+    roof = {"bound": "fp32", "kernel": "k_eval (field evaluation at MIS samples)",
+            "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
+                           f"({peak_kind}); no tensor-core or HBM bound applies (H3)",
+            "traffic": profile_traffic(args.workload),
+            "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.0f} in-support pairs x 16 flop",
+            "eval_ms_per_launch": eval_ms_launch, "eval_share_of_step": float(np.mean(eval_ms)) / (ms / args.steps)}
+    if clocks.get("sm_mhz"):
+        roof["frac_at_sampled_clock"] = achieved / (sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, nt, m, dt, _ = cpu_reference_sample(wl, pos, omega_d.cpu().numpy(), args.cpu_budget)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": nt, "kind": "port",
+               "sample": f"{m} random targets ({dt:.1f} s), both signs, aux=0, Euler update, reference CPU "
+                         f"estimator (monte_carlo_bs_cpu restated in oracle/, bit-exact), OpenMP over targets"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Taylor-Green lattice, strengths from CG-RBF)",
+        "config": {"workload": args.workload, **wl, "N": N, "law": args.law, "k_walk": geo["k_walk"],
+                   "cells_per_axis": geo["cells_x"], "chunks_per_step": geo["chunks"],
+                   "queries_per_thread": sim.tuning()[1],
+                   "l2": "inputs larger than L2 (4.3 GB of sample records + 67 MB candidates per step)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": int(stats["launches_per_step"] * args.steps),
+        "accuracy": err,
+        "cg": {**cg, "seconds": t_cg},
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    sim.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="tg2048")
+    ap.add_argument("--law", choices=["unbiased", "reference"], default="unbiased")
+    ap.add_argument("--k", type=int, default=0, help="walk half-width (0 = auto)")
+    ap.add_argument("--qpt", type=int, default=0, help="queries per thread (0 = auto)")
+    ap.add_argument("--cg-iters", type=int, default=300)
+    ap.add_argument("--err-queries", type=int, default=4096)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gpu":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

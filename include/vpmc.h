@@ -247,9 +247,16 @@ uint64_t vpmc_sim_get_step(vpmc_sim* sim);
 int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
 int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
 
-/* Kernels launched by the last vpmc_sim_step / vpmc_sim_velocity call (per
- * step) and the device time of the field-evaluation kernel in it (ms). */
+/* Kernels launched per step by the last captured or eager pass, and the
+ * device time (ms, CUDA events on the context stream) of the field-evaluation
+ * launches of the last step completed by vpmc_sim_step.  No reference
+ * counterpart (instrumentation). */
 int vpmc_sim_last_stats(vpmc_sim* sim, int* launches_per_step, float* eval_ms);
+
+/* Sizes of the step: info[8] = {particles, targets per chunk, chunks per step,
+ * bins, cells per axis (instance 0), walk half-width k, samples per target,
+ * eval launches in the last timed step}.  No reference counterpart. */
+int vpmc_sim_geometry(vpmc_sim* sim, long long* info);
 
 /* ---------------------------------------------------------------- misc */
 /* Philox4x32-10 (Salmon et al., SC'11) block function, host evaluation:

@@ -24,15 +24,22 @@ def test_matvec_matches_fp64(cuda, Nx, hwr):
 
 
 def test_cg_taylor_green_matches_fp64(cuda):
+    """The RBF matrix is indefinite with eigenvalues near zero, so the
+    coefficients are only pinned once the residual is well below 1e-8: the
+    FP64 oracle itself moves by 3e-5 between tol 1e-8 and full convergence but
+    by 1e-7 beyond tol 1e-10.  Coefficient parity is therefore checked at
+    tol 1e-10; the 1e-8 solve is checked through its residuals."""
     from vortexparticlemc_cuda_gb300 import phash as P
     prm = O.SimParam(Nx=64, hwr=4)
     pos = O.lattice(64)
     b = O.taylor_green(pos)
     st = O.OracleState(pos, b, prm)
-    x64, it, rr, tr = O.cg_rbf_f64(st, b, tol=1e-8, max_iter=1000)
     w, info = P.cg_rbf(to_dev(pos, cuda), to_dev(b, cuda), prm.h_w, tol=1e-8, max_iter=1000)
     assert info["converged"] and info["relres"] < 1e-8
     assert info["true_relres"] < 2e-8
+    x64, it, rr, tr = O.cg_rbf_f64(st, b, tol=1e-10, max_iter=3000)
+    w, info = P.cg_rbf(to_dev(pos, cuda), to_dev(b, cuda), prm.h_w, tol=1e-10, max_iter=3000)
+    assert info["converged"] and info["true_relres"] < 2e-10
     w = w.cpu().numpy()
     assert np.abs(w - x64).max() / np.abs(x64).max() < 1e-5
     # first iteration already removes everything but FP32 rounding of b

@@ -382,7 +382,9 @@ struct vpmc_sim {
     cudaGraphExec_t graph_vel = nullptr;
     int launches_per_step = 0;
     float eval_ms = 0.f;
+    int eval_launches = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> chunk_ev;   // start/end pair per chunk around the eval launch
 };
 
 namespace {
@@ -435,6 +437,10 @@ int alloc_work(vpmc_sim* s) {
     if (per_chunk > s->N) per_chunk = s->N;
     s->chunk_targets = per_chunk;
     const long ns = per_chunk * Q2;
+    const size_t nchunks = size_t((s->N + per_chunk - 1) / per_chunk);
+    for (auto e : s->chunk_ev) cudaEventDestroy(e);
+    s->chunk_ev.assign(2 * nchunks, nullptr);
+    for (auto& e : s->chunk_ev) VPMC_CUDA(cudaEventCreate(&e));
     auto carve_all = [&](Carver& c) {
         carve_grid(c, s->N, nb, s->n_inst, &s->g);
         carve_items(c, nb, ns, &s->it);
@@ -477,15 +483,10 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         L.mode = s->mc[0].law == VPMC_LAW_UNBIASED ? EVAL_FIELD9 : EVAL_FIELD;
         L.qpt = s->qpt;
         L.out_f32 = s->fv;
-        if (timed) VPMC_CUDA(cudaEventRecord(s->ev[0], st));
+        const size_t ci = size_t(t0 / s->chunk_targets);
+        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, cudaEventRecordExternal));
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
-        if (timed) {
-            VPMC_CUDA(cudaEventRecord(s->ev[1], st));
-            VPMC_CUDA(cudaEventSynchronize(s->ev[1]));
-            float ms = 0.f;
-            VPMC_CUDA(cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
-            ms_total += ms;
-        }
+        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, cudaEventRecordExternal));
         AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
                    s->pos_next};
         VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
@@ -494,8 +495,25 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
         VPMC_LAUNCH(k_inc_step, 1, 1, 0, st, s->d_step);
     }
-    if (timed) s->eval_ms = ms_total;
+    (void)ms_total;
     *nlaunch = int(vpmc_kernel_launch_count() - l0);
+    return VPMC_OK;
+}
+
+// Device time of the eval launches of the last completed pass (call after a sync).
+int collect_eval_time(vpmc_sim* s) {
+    const long nchunks = (s->N + s->chunk_targets - 1) / s->chunk_targets;
+    float tot = 0.f;
+    for (long c = 0; c < nchunks; ++c) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->chunk_ev[2 * c], s->chunk_ev[2 * c + 1]) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return VPMC_OK;   // events not recorded (no timed pass yet)
+        }
+        tot += ms;
+    }
+    s->eval_ms = tot;
+    s->eval_launches = int(nchunks);
     return VPMC_OK;
 }
 
@@ -516,12 +534,12 @@ int run_pass(vpmc_sim* s, bool advect, int use_graph) {
     if (!*gx) {
         // eager pass first (sets kernel attributes, sizes the eval grid), then capture
         int nl = 0;
-        VPMC_TRY(issue_pass(s, advect, false, &nl));
+        VPMC_TRY(issue_pass(s, advect, true, &nl));
         VPMC_CUDA(cudaStreamSynchronize(st));
         if (advect) s->step += 1;
         cudaGraph_t graph = nullptr;
         VPMC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int rc = issue_pass(s, advect, false, &nl);
+        const int rc = issue_pass(s, advect, true, &nl);
         const cudaError_t ce = cudaStreamEndCapture(st, &graph);
         if (rc != VPMC_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
         VPMC_CUDA(ce);
@@ -631,6 +649,7 @@ int vpmc_sim_destroy(vpmc_sim* s) {
     cudaStreamSynchronize(s->ctx->stream);
     drop_graphs(s);
     for (auto& e : s->ev) if (e) cudaEventDestroy(e);
+    for (auto e : s->chunk_ev) if (e) cudaEventDestroy(e);
     s->mem.release();
     s->work.release();
     delete s;
@@ -733,7 +752,8 @@ int vpmc_sim_step(vpmc_sim* s, int nsteps, int use_graph) {
     if (!s || nsteps < 0) return VPMC_ERR_INVALID;
     VPMC_CUDA(cudaSetDevice(s->ctx->device));
     for (int k = 0; k < nsteps; ++k) VPMC_TRY(run_pass(s, true, use_graph));
-    return vpmc_context_sync(s->ctx);
+    VPMC_TRY(vpmc_context_sync(s->ctx));
+    return collect_eval_time(s);
 }
 
 int vpmc_sim_velocity(vpmc_sim* s, uint64_t step, float* vel) {
@@ -806,6 +826,19 @@ int vpmc_sim_last_stats(vpmc_sim* s, int* launches_per_step, float* eval_ms) {
     if (!s) return VPMC_ERR_INVALID;
     if (launches_per_step) *launches_per_step = s->launches_per_step;
     if (eval_ms) *eval_ms = s->eval_ms;
+    return VPMC_OK;
+}
+
+int vpmc_sim_geometry(vpmc_sim* s, long long* info) {
+    if (!s || !info) return VPMC_ERR_INVALID;
+    info[0] = s->N;
+    info[1] = s->chunk_targets;
+    info[2] = (s->N + s->chunk_targets - 1) / s->chunk_targets;
+    info[3] = s->g.nbins;
+    info[4] = s->plan.empty() ? 0 : s->plan[0].gx;
+    info[5] = s->plan.empty() ? 0 : s->plan[0].k;
+    info[6] = 2LL * (s->N1 + s->N2);
+    info[7] = s->eval_launches;
     return VPMC_OK;
 }
 

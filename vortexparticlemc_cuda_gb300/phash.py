@@ -358,6 +358,12 @@ class Simulation:
         check(lib().vpmc_sim_get_tuning(self.h, C.byref(k), C.byref(q)), "vpmc_sim_get_tuning")
         return k.value, q.value
 
+    def geometry(self):
+        g = (C.c_longlong * 8)()
+        check(lib().vpmc_sim_geometry(self.h, C.cast(g, C.c_void_p)), "vpmc_sim_geometry")
+        keys = ("N", "chunk_targets", "chunks", "bins", "cells_x", "k_walk", "samples_per_target", "eval_launches")
+        return dict(zip(keys, [int(v) for v in g]))
+
     def last_stats(self):
         n, ms = C.c_int(), C.c_float()
         check(lib().vpmc_sim_last_stats(self.h, C.byref(n), C.byref(ms)), "vpmc_sim_last_stats")
