@@ -231,10 +231,13 @@ def run_gpu(args, wl):
         sim.set_tuning(args.k, args.qpt)
     pos_d = torch.from_numpy(pos).to(dev)
     sim.set_particles(pos_d, torch.zeros(N, device=dev))
+    log = (lambda m: print(f"[bench {time.strftime('%H:%M:%S')}] {m}", file=sys.stderr, flush=True))  # noqa: E731
+    log(f"workload {args.workload}: N={N}, CG init (max {args.cg_iters} iterations)")
     t_cg = time.perf_counter()
     cg = sim.init_strengths(None, tol=1e-8, max_iter=args.cg_iters)[0]
     t_cg = time.perf_counter() - t_cg
     _, omega_d, _ = sim.particles()
+    log(f"CG done in {t_cg:.1f} s: {cg}")
 
     # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
     # sum at 4096 random particles (seed 2)
@@ -253,6 +256,7 @@ def run_gpu(args, wl):
         err = {"vel_rel_rms_vs_fp64_direct": rms / ref, "queries": int(args.err_queries),
                "direct_vs_taylor_green_rel_rms": float(np.sqrt(np.mean(np.sum((truth - tg) ** 2, 1))) / ref)}
 
+    log(f"accuracy: {err}")
     geo = sim.geometry()
     sim.set_step(0)
     sim.step(args.warmup, use_graph=True)
@@ -272,6 +276,7 @@ def run_gpu(args, wl):
     if world > 1:
         dist.barrier()
     ms = e0.elapsed_time(e1)
+    log(f"timed {args.steps} steps: {ms / args.steps:.1f} ms/step, eval {np.mean(eval_ms):.1f} ms/step")
     stats = sim.last_stats()
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -319,6 +324,7 @@ def run_gpu(args, wl):
     if clocks.get("sm_mhz"):
         roof["frac_at_sampled_clock"] = achieved / (sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
 
+    log(f"e2e {e2e['value']:.3e} particle-steps/s")
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, nt, m, dt, _ = cpu_reference_sample(wl, pos, omega_d.cpu().numpy(), args.cpu_budget)

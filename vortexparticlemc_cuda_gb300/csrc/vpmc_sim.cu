@@ -466,6 +466,10 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     vpmc_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     const uint64_t l0 = vpmc_kernel_launch_count();
+    // inside stream capture the timing events must become graph event nodes
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    VPMC_CUDA(cudaStreamIsCapturing(st, &cap));
+    const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
     const int Q = s->N1 + s->N2;
     float ms_total = 0.f;
@@ -484,9 +488,9 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         L.qpt = s->qpt;
         L.out_f32 = s->fv;
         const size_t ci = size_t(t0 / s->chunk_targets);
-        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, cudaEventRecordExternal));
+        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, ev_flags));
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
-        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, cudaEventRecordExternal));
+        if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, ev_flags));
         AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
                    s->pos_next};
         VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
