@@ -165,6 +165,13 @@ int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b,
                 float* omega_out, float h_w, float Lx, float Ly, int periodic,
                 double tol, int max_iter, double* info);
 
+/* vpmc_cg_rbf with an FP64 right-hand side (device, N doubles): a field
+ * sampled in FP64 keeps its structure (e.g. a lattice Fourier mode stays an
+ * exact eigenvector of A), which its FP32 rounding does not. */
+int vpmc_cg_rbf_f64rhs(vpmc_context* ctx, int N, const float* pos, const double* b,
+                       float* omega_out, float h_w, float Lx, float Ly, int periodic,
+                       double tol, int max_iter, double* info);
+
 /* ------------------------------------------------------ direct sums (a11)
  * biot_savart_naive_kernel, src/cuda/naive_biot_savart.cu:15-40, in FP64.
  * VPMC_DIRECT_PLUMMER: targets are particle indices `tidx` (M of them),
@@ -210,7 +217,8 @@ int vpmc_sim_get_particles(vpmc_sim* sim, float* pos, float* omega, float* vel, 
 /* Simulation::init's strength initialisation (src/vortex_particle_mc.cu:99-105,
  * prepare_rhs_b :237-260, conjugate_gradient_rbf): b = omega_field (device,
  * N floats; NULL = Taylor-Green 4 pi sin(2 pi x) sin(2 pi y), include/
- * analytical_flow.hpp:24-28), solved per instance by vpmc_cg_rbf.
+ * analytical_flow.hpp:24-28, evaluated in FP64), solved per instance by
+ * vpmc_cg_rbf (vpmc_cg_rbf_f64rhs for the Taylor-Green field).
  * info (HOST, may be NULL): 3 doubles per instance as vpmc_cg_rbf. */
 int vpmc_sim_init_strengths(vpmc_sim* sim, const float* omega_field, double tol,
                             int max_iter, double* info);
@@ -243,7 +251,7 @@ int vpmc_sim_set_step(vpmc_sim* sim, uint64_t step);
 uint64_t vpmc_sim_get_step(vpmc_sim* sim);
 
 /* Neighbour-walk tuning: cells per h_w (k >= 1, walk (2k+1)^2 cells) and
- * queries per thread in the field-evaluation kernel (1, 2 or 4).  0 = auto. */
+ * queries per thread in the field-evaluation kernel (4 or 8).  0 = auto. */
 int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
 int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
 

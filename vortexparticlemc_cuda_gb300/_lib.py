@@ -60,6 +60,7 @@ SIGNATURES = {
     "vpmc_query_vorticity": (_i, [_vp, _i, _vp, _vp, _vp, _i, _vp, _i, _i, _i, _f, _f, _f, _i, _vp]),
     "vpmc_rbf_matvec": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _i]),
     "vpmc_cg_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
+    "vpmc_cg_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_direct_velocity_f64": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _d, _i, _vp]),
     "vpmc_sim_create": (_i, [_vp, _i, _vp, _vp, C.POINTER(_vp)]),
     "vpmc_sim_destroy": (_i, [_vp]),

@@ -13,7 +13,7 @@ namespace {
 constexpr int kEvalThreads = 256;
 constexpr int kMaxK = 4;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
-constexpr int kCandCap = 2560;                 // float4 candidates staged per batch (40 KB)
+constexpr int kCandCap = 1664;                 // candidates staged per batch (52 KB: 4 CTAs per SM)
 constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
@@ -67,7 +67,7 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const float* __restr
 __global__ void k_grid_gather(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ start, long n,
                               uint32_t nbins, const float2* __restrict__ pos, const float* __restrict__ omega,
                               const GridInst* __restrict__ inst, int n_inst, int set_mode,
-                              float4* __restrict__ cand) {
+                              Cand* __restrict__ cand) {
     const long nv = start[nbins];
     for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x) {
         const uint32_t i = perm[p];
@@ -76,16 +76,17 @@ __global__ void k_grid_gather(const uint32_t* __restrict__ perm, const uint32_t*
         if (G.periodic) { q.x = wrapf(q.x, G.Lx); q.y = wrapf(q.y, G.Ly); }
         const float w = omega ? omega[i] : 1.f;
         const float wt = (set_mode == SET_ONE_SIGNED ? w : fabsf(w)) * G.two_sigma;
-        cand[p] = make_float4(q.x, q.y, wt, 0.f);
+        cand[p] = Cand{q.x, q.x, q.y, q.y, wt, wt, 0.f, 0.f};
     }
 }
 
-__global__ void k_grid_weights(const double* __restrict__ x, long n, double scale, float4* __restrict__ cand) {
+__global__ void k_grid_weights(const double* __restrict__ x, long n, double scale, Cand* __restrict__ cand) {
     for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += long(gridDim.x) * blockDim.x) {
         const double v = x[p] * scale;
         const float hi = float(v);
-        cand[p].z = hi;
-        cand[p].w = float(v - double(hi));
+        cand[p].w = hi;
+        cand[p].w2 = hi;
+        cand[p].wl = float(v - double(hi));
     }
 }
 
@@ -175,7 +176,7 @@ struct BatchPiece {
 struct EvalArgs {
     const GridInst* inst;
     const uint32_t* cstart;
-    const float4* cand;
+    const Cand* cand;
     const QRec* qrec;
     const Item* items;
     const uint32_t* n_items;
@@ -185,9 +186,36 @@ struct EvalArgs {
     unsigned* flags;
 };
 
+// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction
+// serves two queries.  Operands are 64-bit register pairs {lo, hi}.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk2(float a, float b) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(f2x v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+    f2x r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 template <int MODE, int QPT>
 __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
-    extern __shared__ __align__(128) float4 s_cand[];
+    extern __shared__ __align__(128) Cand s_cand[];
     __shared__ Piece s_pc[kMaxPieces];
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
     __shared__ int s_np, s_nbp, s_cur_piece, s_abort;
@@ -196,6 +224,9 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
+    constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9;
+    constexpr int NP = QPT / 2;   // packed query pairs
+    static_assert(!kPacked || (QPT % 2 == 0), "packed path needs an even query count");
     using Acc = typename std::conditional<kF64, double, float>::type;
 
     const int tid = threadIdx.x;
@@ -293,9 +324,10 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 s_btot = tot;
                 if (tot > 0) {
                     fence_proxy_async_smem();
-                    mbar_arrive_expect_tx(&s_bar, tot * 16u);
+                    mbar_arrive_expect_tx(&s_bar, tot * uint32_t(sizeof(Cand)));
                     for (int b = 0; b < nb; ++b)
-                        bulk_g2s(&s_cand[s_bp[b].soff], &a.cand[s_bp[b].gstart], s_bp[b].cnt * 16u, &s_bar);
+                        bulk_g2s(&s_cand[s_bp[b].soff], &a.cand[s_bp[b].gstart],
+                                 s_bp[b].cnt * uint32_t(sizeof(Cand)), &s_bar);
                 }
             }
             __syncthreads();
@@ -309,22 +341,61 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             for (int b = 0; b < nbp; ++b) {
                 const BatchPiece bp = s_bp[b];
                 const Piece pc = s_pc[bp.piece];
-                float px[QPT], py[QPT];
-                Acc part[QPT];
-#pragma unroll
-                for (int j = 0; j < QPT; ++j) {
-                    px[j] = qx[j] + pc.qdx;
-                    py[j] = qy[j] + pc.qdy;
-                    part[j] = Acc(0);
-                }
-                const float4* cs = s_cand + bp.soff;
+                const Cand* cs = s_cand + bp.soff;
                 const int cnt = int(bp.cnt);
-                if constexpr (kF64) {
+                Acc part[QPT];
+                if constexpr (kPacked) {
+                    // field sum  sum_c w_c * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)  (= W / 2 sigma)
+                    const f2x EPS = pk2(1e-30f, 1e-30f), HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
+                    const f2x A2 = pk2(G.A, G.A), B2 = pk2(G.B, G.B), NIH = pk2(-G.inv_hw, -G.inv_hw);
+                    f2x QX[NP], QY[NP], P[NP];
+#pragma unroll
+                    for (int pr = 0; pr < NP; ++pr) {
+                        QX[pr] = pk2(qx[2 * pr] + pc.qdx, qx[2 * pr + 1] + pc.qdx);
+                        QY[pr] = pk2(qy[2 * pr] + pc.qdy, qy[2 * pr + 1] + pc.qdy);
+                        P[pr] = pk2(0.f, 0.f);
+                    }
+#pragma unroll 2
+                    for (int c = 0; c < cnt; ++c) {
+                        const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
+                        const f2x W = *reinterpret_cast<const f2x*>(&cs[c].w);
+#pragma unroll
+                        for (int pr = 0; pr < NP; ++pr) {
+                            const f2x dx = sub2(XY.x, QX[pr]);
+                            const f2x dy = sub2(XY.y, QY[pr]);
+                            const f2x r2 = fma2(dx, dx, fma2(dy, dy, EPS));
+                            float ra, rb;
+                            up2(r2, ra, rb);
+                            const f2x r = mul2(r2, pk2(rsqrtf(ra), rsqrtf(rb)));
+                            const f2x in = fma2(r2, fma2(A2, r, B2), HALF);
+                            const f2x t = fma2(NIH, r, ONE);
+                            const f2x t3 = mul2(mul2(t, t), t);
+                            float ia, ib, ta, tb;
+                            up2(in, ia, ib);
+                            up2(t3, ta, tb);
+                            P[pr] = fma2(W, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+                        }
+                    }
+#pragma unroll
+                    for (int pr = 0; pr < NP; ++pr) {
+                        float lo, hi;
+                        up2(P[pr], lo, hi);
+                        part[2 * pr] = lo;
+                        part[2 * pr + 1] = hi;
+                    }
+                } else if constexpr (kF64) {
+                    float px[QPT], py[QPT];
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        px[j] = qx[j] + pc.qdx;
+                        py[j] = qy[j] + pc.qdy;
+                        part[j] = Acc(0);
+                    }
                     const double hw = double(G.hw);
                     const float lim = G.hw * G.hw * 1.0001f;
 #pragma unroll 2
                     for (int c = 0; c < cnt; ++c) {
-                        const float4 cv = cs[c];
+                        const Cand cv = cs[c];
 #pragma unroll
                         for (int j = 0; j < QPT; ++j) {
                             const float dx = cv.x - px[j], dy = cv.y - py[j];
@@ -332,25 +403,32 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                                 const double ddx = double(cv.x) - (double(qx[j]) + double(pc.qdx));
                                 const double ddy = double(cv.y) - (double(qy[j]) + double(pc.qdy));
                                 const double r = sqrt(ddx * ddx + ddy * ddy);
-                                part[j] += (double(cv.z) + double(cv.w)) * spline_w_d(r, hw);
+                                part[j] += (double(cv.w) + double(cv.wl)) * spline_w_d(r, hw);
                             }
                         }
                     }
                 } else {
+                    float px[QPT], py[QPT];
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        px[j] = qx[j] + pc.qdx;
+                        py[j] = qy[j] + pc.qdy;
+                        part[j] = Acc(0);
+                    }
                     const float A = G.A, B = G.B, ih = G.inv_hw;
 #pragma unroll 4
                     for (int c = 0; c < cnt; ++c) {
-                        const float4 cv = cs[c];
+                        const float cx = cs[c].x, cy = cs[c].y, cw = cs[c].w;
 #pragma unroll
                         for (int j = 0; j < QPT; ++j) {
-                            const float dx = cv.x - px[j], dy = cv.y - py[j];
+                            const float dx = cx - px[j], dy = cy - py[j];
                             const float r2 = fmaf(dx, dx, fmaf(dy, dy, 1e-30f));
                             const float r = r2 * rsqrtf(r2);
                             const float inner = fmaf(r2, fmaf(A, r, B), 0.5f);
                             const float t = fmaf(-ih, r, 1.0f);
                             float v = fmaxf(fminf(inner, t * t * t), 0.0f);
                             if (MODE == EVAL_FIELD_EXC && r2 < 1e-12f) v = 0.f;
-                            part[j] = fmaf(cv.z, v, part[j]);
+                            part[j] = fmaf(cw, v, part[j]);
                         }
                     }
                 }
@@ -396,7 +474,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 
 template <int MODE, int QPT>
 int launch_eval_t(vpmc_context* ctx, const EvalArgs& a) {
-    const size_t smem = size_t(kCandCap) * sizeof(float4);
+    const size_t smem = size_t(kCandCap) * sizeof(Cand);
     static bool configured[64] = {};
     const int dev = ctx->device;
     if (dev < 64 && !configured[dev]) {
@@ -422,7 +500,7 @@ int blocks_for(long n, int threads = 256) {
 
 int default_k() { return 2; }
 
-int query_chunk(int qpt) { return (qpt == 1 || qpt == 2 ? qpt : 4) * kEvalThreads; }
+int query_chunk(int qpt) { return (qpt == 8 ? 8 : 4) * kEvalThreads; }
 
 long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     if (k <= 0) k = default_k();
@@ -473,7 +551,7 @@ void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g) {
     g->keys = c.take<uint32_t>(size_t(n < 1 ? 1 : n));
     g->count = c.take<uint32_t>(size_t(nbins + 1));
     g->start = c.take<uint32_t>(size_t(nbins + 1));
-    g->cand = c.take<float4>(size_t(n < 1 ? 1 : n));
+    g->cand = c.take<Cand>(size_t(n < 1 ? 1 : n));
     carve_radix(c, n, &g->rs);
     // the bin scan reuses the radix scan scratch when it is large enough
     const size_t need = scan_tmp_elems(nbins + 1);
@@ -549,12 +627,10 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
     EvalArgs a{g.inst, g.start, g.cand, qrec, it.items, it.n_items, it.counter, L.out_f32, L.out_f64, ctx->d_flags};
     switch (L.mode) {
         case EVAL_FIELD:
-            if (L.qpt == 1) return launch_eval_t<EVAL_FIELD, 1>(ctx, a);
-            if (L.qpt == 2) return launch_eval_t<EVAL_FIELD, 2>(ctx, a);
+            if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);
             return launch_eval_t<EVAL_FIELD, 4>(ctx, a);
         case EVAL_FIELD9:
-            if (L.qpt == 1) return launch_eval_t<EVAL_FIELD9, 1>(ctx, a);
-            if (L.qpt == 2) return launch_eval_t<EVAL_FIELD9, 2>(ctx, a);
+            if (L.qpt == 8) return launch_eval_t<EVAL_FIELD9, 8>(ctx, a);
             return launch_eval_t<EVAL_FIELD9, 4>(ctx, a);
         case EVAL_FIELD_EXC:
             if (L.qpt != 4) return VPMC_ERR_INVALID;

@@ -4,7 +4,8 @@
 // RBF SpMV) runs through the same structure:
 //   * particles ("candidates") are sorted stably by bin = (instance, sign set,
 //     cell) on a grid whose cell side s >= h_w / k, and gathered into an AoS
-//     float4 {x, y, weight, weight_lo} array so each cell is one contiguous run;
+//     32-byte record array (coordinates and weight duplicated for packed math)
+//     so each cell is one contiguous run;
 //   * query points are binned by the cell of their wrapped position;
 //   * one CTA takes a bin (or a chunk of it), stages the (2k+1)^2 neighbour
 //     cells -- at most 2(2k+1) contiguous runs, one per column and periodic
@@ -31,6 +32,14 @@ struct GridInst {
     float A, B;             // 3/h_w^3, -3/h_w^2: W/(2 sigma) = min(0.5 + r^2 (A r + B), (1 - r/h_w)^3)
     float two_sigma;        // 2 * 40 / (7 pi h_w^2)
     int p_begin, p_end;     // particle range of the instance
+};
+
+// Candidate record (32 bytes): coordinates and weight duplicated so that one
+// shared-memory broadcast load feeds packed f32x2 operands for two queries.
+// w = weight (FP32 hi part), wl = the FP32 remainder (for FP64 SpMV weights).
+struct __align__(16) Cand {
+    float x, x2, y, y2;
+    float w, w2, wl, pad;
 };
 
 // Query record: wrapped position, output slot, image flags (16 bytes).
@@ -86,7 +95,7 @@ struct GridBufs {
     uint32_t* keys = nullptr;   // n
     uint32_t* count = nullptr;  // nbins + 1
     uint32_t* start = nullptr;  // nbins + 1 (exclusive prefix, start[nbins] = candidates)
-    float4* cand = nullptr;     // n
+    Cand* cand = nullptr;       // n
     uint32_t* perm = nullptr;   // n: sorted slot -> particle (points into rs buffers)
     RadixScratch rs{};
 };
@@ -136,7 +145,7 @@ int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
 
 struct EvalLaunch {
     int mode = EVAL_FIELD;
-    int qpt = 4;               // queries per thread (1, 2, 4)
+    int qpt = 4;               // queries per thread (FIELD modes: 4 or 8; others: 4)
     float* out_f32 = nullptr;
     double* out_f64 = nullptr;
 };

@@ -17,12 +17,12 @@ int blocks_for(long n) {
 
 // Queries = the candidates themselves (RBF SpMV): qrec[p] = cand[p], output
 // slot = sorted slot (use_perm = 0) or original index (use_perm = 1).
-__global__ void k_self_queries(const float4* __restrict__ cand, const uint32_t* __restrict__ perm,
+__global__ void k_self_queries(const Cand* __restrict__ cand, const uint32_t* __restrict__ perm,
                                const uint32_t* __restrict__ start, long n, uint32_t nbins, int use_perm,
                                QRec* __restrict__ q) {
     const long nv = start[nbins];
     for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x) {
-        const float4 c = cand[p];
+        const Cand c = cand[p];
         q[p] = QRec{c.x, c.y, use_perm ? perm[p] : uint32_t(p), (2u) | (2u << 3)};
     }
 }
@@ -31,6 +31,12 @@ __global__ void k_gather_to_sorted(const float* __restrict__ x, const uint32_t* 
                                    double* __restrict__ xs) {
     for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += long(gridDim.x) * blockDim.x)
         xs[p] = double(x[perm[p]]);
+}
+
+__global__ void k_gather_to_sorted_d(const double* __restrict__ x, const uint32_t* __restrict__ perm, long n,
+                                     double* __restrict__ xs) {
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += long(gridDim.x) * blockDim.x)
+        xs[p] = x[perm[p]];
 }
 
 __global__ void k_scatter_from_sorted(const double* __restrict__ xs, const uint32_t* __restrict__ perm, long n,
@@ -180,14 +186,17 @@ int vpmc_rbf_matvec(vpmc_context* ctx, int N, const float* pos, const float* x, 
     return vpmc_context_sync(ctx);
 }
 
-int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, float* omega_out, float h_w, float Lx,
-                float Ly, int periodic, double tol, int max_iter, double* info) {
+}  // extern "C"
+
+namespace {
+int cg_impl(vpmc_context* ctx, int N, const float* pos, const float* b, const double* b64, float* omega_out, float h_w,
+            float Lx, float Ly, int periodic, double tol, int max_iter, double* info) {
     if (!ctx || N < 0 || !(h_w > 0.f) || !(Lx > 0.f) || !(Ly > 0.f) || max_iter < 0) return VPMC_ERR_INVALID;
     if (N == 0) {
         if (info) { info[0] = 0; info[1] = 0; info[2] = 0; }
         return VPMC_OK;
     }
-    if (!pos || !b || !omega_out) return VPMC_ERR_INVALID;
+    if (!pos || (!b && !b64) || !omega_out) return VPMC_ERR_INVALID;
     VPMC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     Work w;
@@ -197,7 +206,8 @@ int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, floa
     VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.start, long(N),
                 uint32_t(w.g.nbins), 0, w.self);
     VPMC_TRY(make_items(ctx, w.g, w.g.start, w.it, query_chunk(4)));
-    VPMC_LAUNCH(k_gather_to_sorted, blocks_for(N), 256, 0, st, b, w.g.perm, long(N), bs);
+    if (b64) VPMC_LAUNCH(k_gather_to_sorted_d, blocks_for(N), 256, 0, st, b64, w.g.perm, long(N), bs);
+    else VPMC_LAUNCH(k_gather_to_sorted, blocks_for(N), 256, 0, st, b, w.g.perm, long(N), bs);
     const double diag = spline_w_d(0.0, double(h_w));   // W(0), the reference's x0 = b / W(0)
     VPMC_LAUNCH(k_axpby, blocks_for(N), 256, 0, st, bs, bs, long(N), 1.0 / diag, 0.0, x);
     VPMC_TRY(spmv_sorted(ctx, w, x, Ap, true));
@@ -237,5 +247,22 @@ int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, floa
     }
     return res < tol || bnorm == 0 ? VPMC_OK : VPMC_ERR_NOT_CONVERGED;
 }
+}  // namespace
+
+extern "C" {
+
+int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, float* omega_out, float h_w, float Lx,
+                float Ly, int periodic, double tol, int max_iter, double* info) {
+    if (!b && N > 0) return VPMC_ERR_INVALID;
+    return cg_impl(ctx, N, pos, b, nullptr, omega_out, h_w, Lx, Ly, periodic, tol, max_iter, info);
+}
+
+int vpmc_cg_rbf_f64rhs(vpmc_context* ctx, int N, const float* pos, const double* b, float* omega_out, float h_w,
+                       float Lx, float Ly, int periodic, double tol, int max_iter, double* info) {
+    if (!b && N > 0) return VPMC_ERR_INVALID;
+    return cg_impl(ctx, N, pos, nullptr, b, omega_out, h_w, Lx, Ly, periodic, tol, max_iter, info);
+}
+
+
 
 }  // extern "C"

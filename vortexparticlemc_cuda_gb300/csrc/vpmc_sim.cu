@@ -299,10 +299,14 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
 
 __global__ void k_inc_step(unsigned long long* s) { *s += 1ull; }
 
-__global__ void k_taylor_green(const float2* __restrict__ pos, long n, float* __restrict__ b) {
+// taylor_green_vorticity (include/analytical_flow.hpp:24-28) evaluated in
+// FP64: on a lattice the FP64 field is an exact eigenvector of the RBF matrix,
+// which an FP32-rounded copy is not (its rounding spreads over eigenvalues
+// near zero and stalls CG near 1e-6 at 2048^2).
+__global__ void k_taylor_green(const float2* __restrict__ pos, long n, double* __restrict__ b) {
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
         const double x = pos[i].x, y = pos[i].y;
-        b[i] = float(4.0 * kPiD * sin(2.0 * kPiD * x) * sin(2.0 * kPiD * y));
+        b[i] = 4.0 * kPiD * sin(2.0 * kPiD * x) * sin(2.0 * kPiD * y);
     }
 }
 
@@ -729,10 +733,11 @@ int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, i
     vpmc_context* ctx = s->ctx;
     VPMC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    float* b = nullptr;
+    double* b = nullptr;
     if (!omega_field) {
-        b = s->fv;   // reuse sample-value scratch for the right-hand side (>= N floats)
-        if (s->max_samples < s->N) return VPMC_ERR_CAPACITY;
+        // reuse the sample-position scratch for the FP64 right-hand side
+        b = reinterpret_cast<double*>(s->ys);
+        if (s->chunk_targets * 2L * (s->N1 + s->N2) < s->N) return VPMC_ERR_CAPACITY;
         VPMC_LAUNCH(k_taylor_green, blocks_for(s->N), 256, 0, st, s->pos, s->N, b);
     }
     int worst = VPMC_OK;
@@ -740,9 +745,13 @@ int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, i
         const long off = s->begin[i];
         const vpmc_sim_params& p = s->prm[i];
         double inf[3] = {0, 0, 0};
-        const float* bi = omega_field ? omega_field + off : b + off;
-        const int rc = vpmc_cg_rbf(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off), bi,
-                                   s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol, max_iter, inf);
+        const int rc = omega_field
+                           ? vpmc_cg_rbf(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off),
+                                         omega_field + off, s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol,
+                                         max_iter, inf)
+                           : vpmc_cg_rbf_f64rhs(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off),
+                                                b + off, s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol,
+                                                max_iter, inf);
         if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) return rc;
         if (rc != VPMC_OK) worst = rc;
         if (info) { info[3 * i] = inf[0]; info[3 * i + 1] = inf[1]; info[3 * i + 2] = inf[2]; }
@@ -812,7 +821,7 @@ int vpmc_sim_set_step(vpmc_sim* s, uint64_t step) {
 uint64_t vpmc_sim_get_step(vpmc_sim* s) { return s ? s->step : 0; }
 
 int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
-    if (!s || k_walk < 0 || k_walk > 4 || !(qpt == 0 || qpt == 1 || qpt == 2 || qpt == 4)) return VPMC_ERR_INVALID;
+    if (!s || k_walk < 0 || k_walk > 4 || !(qpt == 0 || qpt == 4 || qpt == 8)) return VPMC_ERR_INVALID;
     s->k_walk = k_walk;
     s->qpt = qpt == 0 ? 4 : qpt;
     VPMC_TRY(alloc_work(s));
