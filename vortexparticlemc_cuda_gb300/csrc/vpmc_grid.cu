@@ -213,6 +213,36 @@ __device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
     return r;
 }
 
+// sum over one staged run of candidates for NPR packed query pairs:
+// P[pr] += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)   (= w * W / 2 sigma)
+template <int NPR, int NPMAX>
+__device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
+                                           const f2x (&QY)[NPMAX], f2x (&P)[NPMAX], float A, float B, float ih) {
+    const f2x EPS = pk2(1e-30f, 1e-30f), HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
+    const f2x A2 = pk2(A, A), B2 = pk2(B, B), NIH = pk2(-ih, -ih);
+#pragma unroll 2
+    for (int c = 0; c < cnt; ++c) {
+        const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
+        const f2x W = *reinterpret_cast<const f2x*>(&cs[c].w);
+#pragma unroll
+        for (int pr = 0; pr < NPR; ++pr) {
+            const f2x dx = sub2(XY.x, QX[pr]);
+            const f2x dy = sub2(XY.y, QY[pr]);
+            const f2x r2 = fma2(dx, dx, fma2(dy, dy, EPS));
+            float ra, rb;
+            up2(r2, ra, rb);
+            const f2x r = mul2(r2, pk2(rsqrtf(ra), rsqrtf(rb)));
+            const f2x in = fma2(r2, fma2(A2, r, B2), HALF);
+            const f2x t = fma2(NIH, r, ONE);
+            const f2x t3 = mul2(mul2(t, t), t);
+            float ia, ib, ta, tb;
+            up2(in, ia, ib);
+            up2(t3, ta, tb);
+            P[pr] = fma2(W, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+        }
+    }
+}
+
 template <int MODE, int QPT>
 __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     extern __shared__ __align__(128) Cand s_cand[];
@@ -245,6 +275,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
         if (item >= *a.n_items) break;
         const Item it = a.items[item];
         const GridInst G = a.inst[it.inst];
+        const int nq = int((it.qcnt + kEvalThreads - 1) / kEvalThreads);   // queries per thread this item
 
         if (tid == 0) {
             const uint32_t local = it.bin - uint32_t(G.bin_base);
@@ -345,9 +376,6 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 const int cnt = int(bp.cnt);
                 Acc part[QPT];
                 if constexpr (kPacked) {
-                    // field sum  sum_c w_c * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)  (= W / 2 sigma)
-                    const f2x EPS = pk2(1e-30f, 1e-30f), HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
-                    const f2x A2 = pk2(G.A, G.A), B2 = pk2(G.B, G.B), NIH = pk2(-G.inv_hw, -G.inv_hw);
                     f2x QX[NP], QY[NP], P[NP];
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
@@ -355,27 +383,10 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                         QY[pr] = pk2(qy[2 * pr] + pc.qdy, qy[2 * pr + 1] + pc.qdy);
                         P[pr] = pk2(0.f, 0.f);
                     }
-#pragma unroll 2
-                    for (int c = 0; c < cnt; ++c) {
-                        const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
-                        const f2x W = *reinterpret_cast<const f2x*>(&cs[c].w);
-#pragma unroll
-                        for (int pr = 0; pr < NP; ++pr) {
-                            const f2x dx = sub2(XY.x, QX[pr]);
-                            const f2x dy = sub2(XY.y, QY[pr]);
-                            const f2x r2 = fma2(dx, dx, fma2(dy, dy, EPS));
-                            float ra, rb;
-                            up2(r2, ra, rb);
-                            const f2x r = mul2(r2, pk2(rsqrtf(ra), rsqrtf(rb)));
-                            const f2x in = fma2(r2, fma2(A2, r, B2), HALF);
-                            const f2x t = fma2(NIH, r, ONE);
-                            const f2x t3 = mul2(mul2(t, t), t);
-                            float ia, ib, ta, tb;
-                            up2(in, ia, ib);
-                            up2(t3, ta, tb);
-                            P[pr] = fma2(W, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
-                        }
-                    }
+                    // an item with few queries runs fewer pairs per thread (uniform per CTA)
+                    if (nq <= 2) packed_run<1, NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
+                    else if (NP >= 2 && nq <= 4) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
+                    else packed_run<NP, NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;

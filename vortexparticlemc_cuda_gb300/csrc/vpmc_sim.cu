@@ -590,7 +590,7 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
     s->N = N;
     s->N1 = prms[0].N1;
     s->N2 = prms[0].N2;
-    s->max_samples = 1L << 27;
+    s->max_samples = 1L << 29;   // sample records per chunk (32 B each): fuller bins, fewer passes
     long b = 0;
     s->mc.resize(n_inst);
     for (int i = 0; i < n_inst; ++i) {
