@@ -202,6 +202,11 @@ __device__ __forceinline__ f2x sub2(f2x a, f2x b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+    f2x r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ f2x mul2(f2x a, f2x b) {
     f2x r;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
@@ -213,32 +218,45 @@ __device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
     return r;
 }
 
-// sum over one staged run of candidates for NPR packed query pairs:
-// P[pr] += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)   (= w * W / 2 sigma)
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Sum over one staged run of candidates for NPR packed query pairs, in
+// bin-local coordinates: candidates hold (x, y) relative to the bin centre
+// and c2 = x^2 + y^2; queries enter as -2 q and |q|^2, so
+//   r^2 = max(c2 + q2 - 2 c.q, 0),  r = sqrt(r^2)
+//   P  += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)      (= w W / 2 sigma)
+// 9 FMA-pipe operations per pair (2 per query of r^2 setup, 1 sqrt on the XU).
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
-                                           const f2x (&QY)[NPMAX], f2x (&P)[NPMAX], float A, float B, float ih) {
-    const f2x EPS = pk2(1e-30f, 1e-30f), HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
+                                           const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX],
+                                           float A, float B, float ih) {
+    const f2x HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
     const f2x A2 = pk2(A, A), B2 = pk2(B, B), NIH = pk2(-ih, -ih);
 #pragma unroll 2
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
-        const f2x W = *reinterpret_cast<const f2x*>(&cs[c].w);
+        const ulonglong2 WC = *reinterpret_cast<const ulonglong2*>(&cs[c].w);   // (w, w), (c2, c2)
 #pragma unroll
         for (int pr = 0; pr < NPR; ++pr) {
-            const f2x dx = sub2(XY.x, QX[pr]);
-            const f2x dy = sub2(XY.y, QY[pr]);
-            const f2x r2 = fma2(dx, dx, fma2(dy, dy, EPS));
+            const f2x s = add2(WC.y, Q2[pr]);
+            const f2x r2p = fma2(XY.y, QY[pr], fma2(XY.x, QX[pr], s));
             float ra, rb;
-            up2(r2, ra, rb);
-            const f2x r = mul2(r2, pk2(rsqrtf(ra), rsqrtf(rb)));
+            up2(r2p, ra, rb);
+            ra = fmaxf(ra, 0.f);
+            rb = fmaxf(rb, 0.f);
+            const f2x r2 = pk2(ra, rb);
+            const f2x r = pk2(sqrt_approx(ra), sqrt_approx(rb));
             const f2x in = fma2(r2, fma2(A2, r, B2), HALF);
             const f2x t = fma2(NIH, r, ONE);
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
             up2(in, ia, ib);
             up2(t3, ta, tb);
-            P[pr] = fma2(W, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+            P[pr] = fma2(WC.x, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
         }
     }
 }
@@ -250,6 +268,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
     __shared__ int s_np, s_nbp, s_cur_piece, s_abort;
     __shared__ uint32_t s_cur_off, s_btot, s_item;
+    __shared__ float s_ox, s_oy;
     __shared__ __align__(8) uint64_t s_bar;
 
     constexpr bool kF64 = MODE == EVAL_SPMV64;
@@ -311,6 +330,9 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             s_np = np;
             s_cur_piece = 0;
             s_cur_off = 0;
+            // bin centre (wrapped coordinates): origin of the local frame
+            s_ox = (float(cx) + 0.5f) / G.inv_sx;
+            s_oy = (float(cy) + 0.5f) / G.inv_sy;
         }
 
         // this thread's queries
@@ -369,6 +391,26 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             if (s_abort) break;
 
             const int nbp = s_nbp;
+            if constexpr (kPacked) {
+                // staged candidates -> image-shifted, bin-local coordinates + c2
+                for (int b = 0; b < nbp; ++b) {
+                    const BatchPiece bp = s_bp[b];
+                    const Piece pc = s_pc[bp.piece];
+                    const float ox = s_ox + pc.qdx, oy = s_oy + pc.qdy;
+                    for (uint32_t c = threadIdx.x; c < bp.cnt; c += kEvalThreads) {
+                        Cand& cd = s_cand[bp.soff + c];
+                        const float lx = cd.x - ox, ly = cd.y - oy;
+                        const float c2 = fmaf(lx, lx, ly * ly);
+                        cd.x = lx;
+                        cd.x2 = lx;
+                        cd.y = ly;
+                        cd.y2 = ly;
+                        cd.wl = c2;
+                        cd.pad = c2;
+                    }
+                }
+                __syncthreads();
+            }
             for (int b = 0; b < nbp; ++b) {
                 const BatchPiece bp = s_bp[b];
                 const Piece pc = s_pc[bp.piece];
@@ -376,17 +418,21 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 const int cnt = int(bp.cnt);
                 Acc part[QPT];
                 if constexpr (kPacked) {
-                    f2x QX[NP], QY[NP], P[NP];
+                    // queries in the same local frame: -2 q and |q|^2
+                    f2x QX[NP], QY[NP], Q2[NP], P[NP];
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
-                        QX[pr] = pk2(qx[2 * pr] + pc.qdx, qx[2 * pr + 1] + pc.qdx);
-                        QY[pr] = pk2(qy[2 * pr] + pc.qdy, qy[2 * pr + 1] + pc.qdy);
+                        const float ax = qx[2 * pr] - s_ox, bx = qx[2 * pr + 1] - s_ox;
+                        const float ay = qy[2 * pr] - s_oy, by = qy[2 * pr + 1] - s_oy;
+                        QX[pr] = pk2(-2.f * ax, -2.f * bx);
+                        QY[pr] = pk2(-2.f * ay, -2.f * by);
+                        Q2[pr] = pk2(fmaf(ax, ax, ay * ay), fmaf(bx, bx, by * by));
                         P[pr] = pk2(0.f, 0.f);
                     }
                     // an item with few queries runs fewer pairs per thread (uniform per CTA)
-                    if (nq <= 2) packed_run<1, NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
-                    else if (NP >= 2 && nq <= 4) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
-                    else packed_run<NP, NP>(cs, cnt, QX, QY, P, G.A, G.B, G.inv_hw);
+                    if (nq <= 2) packed_run<1, NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
+                    else if (NP >= 2 && nq <= 4) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
+                    else packed_run<NP, NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;
