@@ -114,6 +114,25 @@ int vpmc_hash_build_host(vpmc_context* ctx, int rshx, int rshy, float Lx, float 
                          int n_pos, const int* sub, const float* pos, int* cell_num,
                          int* cell_acc, int* vp_cell, int* vp_sort);
 
+/* Allocation-free variant of vpmc_hash_build, with no counterpart in the
+ * reference.  For callers that cannot allocate device memory -- a host
+ * application that owns all device memory and forbids plugins to call
+ * cudaMalloc, or a real-time loop that cannot take cudaMalloc's implicit
+ * device synchronisation.  No context: work runs on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream) and the call returns when it is done.
+ * It calls no cudaMalloc/cudaFree and no allocating library routine; its
+ * radix-sort and scan scratch is a fixed ~4.3 MB __device__ array inside the
+ * library that every GPU using the library holds until process exit.
+ * Limits: N <= 262144 particles and rshx*rshy <= 1048576 cells, otherwise
+ * VPMC_ERR_CAPACITY.  All calls share that scratch, so calls that overlap on
+ * the GPU (two host threads, or two streams) race; consecutive calls are
+ * safe.  The first call on a device looks up the scratch array's address:
+ * make it before any stream capture.  Results are identical to
+ * vpmc_hash_build (device pointers, same layouts). */
+int vpmc_hash_build_noalloc(void* stream, int rshx, int rshy, float Lx, float Ly, int N,
+                            const int* sub, const float* pos, int* cell_num, int* cell_acc,
+                            int* vp_cell, int* vp_sort);
+
 /* --------------------------------------------------------------- subsets (a4)
  * build_subsets_cuda, src/cuda/build_particle_sets.cu:11-89: split particle
  * indices by the sign of omega (zeros belong to neither), |omega| prefix sums

@@ -54,6 +54,7 @@ SIGNATURES = {
     "vpmc_counting_sort": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
     "vpmc_hash_build": (_i, [_vp, _i, _i, _f, _f, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "vpmc_hash_build_host": (_i, [_vp, _i, _i, _f, _f, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "vpmc_hash_build_noalloc": (_i, [_vp, _i, _i, _f, _f, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "vpmc_build_subsets": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "vpmc_kernel_icdf_table": (_i, [_f, _i, _vp, _vp]),
     "vpmc_cubic_spline": (_f, [_f, _f]),

@@ -169,6 +169,16 @@ size_t dscan_tmp_elems(long n) {
 
 }  // namespace
 
+// FillCells kernel on a caller-given stream, no context and no allocation
+// (used by the allocation-free hash entry point).  cell_num must be zeroed.
+int launch_fill_cells(cudaStream_t st, int rshx, int rshy, float inv_hx, float inv_hy, const int* sub,
+                      const float2* pos, long N, int* cell_num, int* vp_cell) {
+    if (N <= 0) return VPMC_OK;
+    VPMC_LAUNCH(k_fill_cells, blocks_for(N), kHashThreads, 0, st, rshx, rshy, inv_hx, inv_hy, sub, pos, N, cell_num,
+                vp_cell);
+    return VPMC_OK;
+}
+
 // Subset build shared with the simulation: writes sub/abs values, returns
 // counts and totals (host), CDF normalised in place.  Device scratch from `c`.
 int build_subsets_dev(vpmc_context* ctx, long N, const float* omega, int* sub_pos, int* sub_neg, double* cdf_pos,
