@@ -227,8 +227,7 @@ def run_gpu(args, wl):
     N = len(pos)
     sp = P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=rank)
     sim = P.Simulation(sp, [N])
-    if args.k or args.qpt:
-        sim.set_tuning(args.k, args.qpt)
+    tune = None
     pos_d = torch.from_numpy(pos).to(dev)
     sim.set_particles(pos_d, torch.zeros(N, device=dev))
     log = (lambda m: print(f"[bench {time.strftime('%H:%M:%S')}] {m}", file=sys.stderr, flush=True))  # noqa: E731
@@ -257,6 +256,14 @@ def run_gpu(args, wl):
                "direct_vs_taylor_green_rel_rms": float(np.sqrt(np.mean(np.sum((truth - tg) ** 2, 1))) / ref)}
 
     log(f"accuracy: {err}")
+    if args.k or args.qpt:
+        sim.set_tuning(args.k, args.qpt)
+    else:
+        t_t = time.perf_counter()
+        k_sel, q_sel, best = sim.autotune()
+        tune = {"k_walk": k_sel, "queries_per_thread": q_sel, "best_pass_ms": best,
+                "seconds": time.perf_counter() - t_t}
+        log(f"autotune: {tune}")
     geo = sim.geometry()
     sim.set_step(0)
     sim.step(args.warmup, use_graph=True)
@@ -349,6 +356,7 @@ def run_gpu(args, wl):
         "gpu_launches": int(stats["launches_per_step"] * args.steps),
         "accuracy": err,
         "cg": {**cg, "seconds": t_cg},
+        "autotune": tune,
     }
     if rank == 0:
         print(json.dumps(out))

@@ -274,6 +274,14 @@ uint64_t vpmc_sim_get_step(vpmc_sim* sim);
 int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
 int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
 
+/* Autotuner (no reference counterpart): times one full MIS velocity pass per
+ * candidate (k_walk, queries_per_thread) in {2,3,4}x{4} + {2,3}x{8}, keeps
+ * the fastest, and caches the choice in-process by (hwr, samples per target,
+ * particles per h_w^2).  Results do not depend on the choice beyond FP32
+ * rounding of the field sums.  Outputs (HOST, may be NULL): chosen k,
+ * queries per thread, and the best pass time in ms (-1 when cached). */
+int vpmc_sim_autotune(vpmc_sim* sim, int* k_walk, int* queries_per_thread, float* best_ms);
+
 /* Kernels launched per step by the last captured or eager pass, and the
  * device time (ms, CUDA events on the context stream) of the field-evaluation
  * launches of the last step completed by vpmc_sim_step.  No reference

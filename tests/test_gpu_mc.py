@@ -152,6 +152,18 @@ def test_tuning_does_not_change_results_beyond_rounding(cuda):
         assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max(), (k, q)
 
 
+def test_autotune_picks_a_candidate_and_caches(cuda):
+    sim, pos, om, prm = _setup(cuda, law=1)
+    base = sim.velocity(step=2).cpu().numpy()
+    k, q, ms = sim.autotune()
+    assert k in (2, 3, 4) and q in (4, 8) and ms > 0
+    assert sim.tuning() == (k, q)
+    v = sim.velocity(step=2).cpu().numpy()
+    assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max()
+    sim2, *_ = _setup(cuda, law=1)
+    assert sim2.autotune() == (k, q, -1.0)     # cached by shape
+
+
 def test_empty_sign_subset(cuda):
     """All strengths positive: the negative branch contributes nothing (the
     reference would index sub[-1])."""

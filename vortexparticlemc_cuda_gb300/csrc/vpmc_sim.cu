@@ -21,7 +21,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "vpmc_grid.cuh"
@@ -825,6 +828,61 @@ int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
     s->k_walk = k_walk;
     s->qpt = qpt == 0 ? 4 : qpt;
     VPMC_TRY(alloc_work(s));
+    return vpmc_context_sync(s->ctx);
+}
+
+// Autotuner: time one full velocity pass (gen + bin + eval + accumulate) for
+// each candidate (cells per h_w, queries per thread) and keep the fastest.
+// Results are cached in-process by (hwr, samples per target, particles per
+// h_w^2 of instance 0), so a second simulation of the same shape reuses them.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tune_cache;
+}  // namespace
+
+int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
+    if (!s) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
+    const vpmc_sim_params& p = s->prm[0];
+    const double density = double(s->counts[0]) / (double(p.Lx) * p.Ly) * double(s->mc[0].hw) * s->mc[0].hw;
+    const auto key = std::make_tuple(int(std::lround(p.hwr * 16)), s->N1 + s->N2, int(std::lround(density)));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            VPMC_TRY(vpmc_sim_set_tuning(s, it->second.first, it->second.second));
+            if (k_out) *k_out = s->plan[0].k;
+            if (qpt_out) *qpt_out = s->qpt;
+            if (best_ms) *best_ms = -1.f;
+            return VPMC_OK;
+        }
+    }
+    cudaStream_t st = s->ctx->stream;
+    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {2, 8}, {3, 8}};
+    float best = 1e30f;
+    int bk = 0, bq = 4;
+    for (const auto& c : cands) {
+        if (vpmc_sim_set_tuning(s, c[0], c[1]) != VPMC_OK) continue;
+        if (s->plan[0].k != c[0]) continue;   // geometry clamped k: skip duplicates
+        int nl = 0;
+        VPMC_TRY(issue_pass(s, false, false, &nl));   // warm (kernel attributes, caches)
+        VPMC_CUDA(cudaEventRecord(s->ev[0], st));
+        VPMC_TRY(issue_pass(s, false, false, &nl));
+        VPMC_CUDA(cudaEventRecord(s->ev[1], st));
+        VPMC_CUDA(cudaEventSynchronize(s->ev[1]));
+        float ms = 0.f;
+        VPMC_CUDA(cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
+        if (ms < best) { best = ms; bk = c[0]; bq = c[1]; }
+    }
+    VPMC_TRY(vpmc_sim_set_tuning(s, bk, bq));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = {bk, bq};
+    }
+    if (k_out) *k_out = s->plan[0].k;
+    if (qpt_out) *qpt_out = s->qpt;
+    if (best_ms) *best_ms = best;
     return vpmc_context_sync(s->ctx);
 }
 

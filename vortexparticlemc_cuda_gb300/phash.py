@@ -353,6 +353,12 @@ class Simulation:
     def set_tuning(self, k_walk: int = 0, queries_per_thread: int = 0):
         check(lib().vpmc_sim_set_tuning(self.h, int(k_walk), int(queries_per_thread)), "vpmc_sim_set_tuning")
 
+    def autotune(self):
+        """Pick (k_walk, queries_per_thread) by timing; returns (k, qpt, best pass ms or -1 if cached)."""
+        k, q, ms = C.c_int(), C.c_int(), C.c_float()
+        check(lib().vpmc_sim_autotune(self.h, C.byref(k), C.byref(q), C.byref(ms)), "vpmc_sim_autotune")
+        return k.value, q.value, ms.value
+
     def tuning(self):
         k, q = C.c_int(), C.c_int()
         check(lib().vpmc_sim_get_tuning(self.h, C.byref(k), C.byref(q)), "vpmc_sim_get_tuning")
