@@ -263,6 +263,13 @@ int vpmc_sim_velocity(vpmc_sim* sim, uint64_t step, float* vel);
  * copies positions and velocities back (2N each). */
 int vpmc_sim_step_host(vpmc_sim* sim, const float* pos_in, float* pos_out, float* vel_out);
 
+/* Forward-Euler update with the FP64 periodic wrap, x += dt*u (the position
+ * update of Simulation::step_cuda / step_cuda_naive, src/cuda/simulation_step.cu:
+ * 77-89, 115-128).  Velocities come from vel (float2) or, if vel is NULL, from
+ * vel64 (double2).  Device pointers. */
+int vpmc_advect(vpmc_context* ctx, int N, float* pos, const float* vel, const double* vel64, float dt,
+                float Lx, float Ly, int periodic);
+
 /* Change the estimator law / seed / step counter of an existing simulation. */
 int vpmc_sim_set_law(vpmc_sim* sim, int law);
 int vpmc_sim_set_seed(vpmc_sim* sim, uint64_t seed);

@@ -73,6 +73,7 @@ SIGNATURES = {
     "vpmc_sim_step": (_i, [_vp, _i, _i]),
     "vpmc_sim_velocity": (_i, [_vp, _u64, _vp]),
     "vpmc_sim_step_host": (_i, [_vp, _vp, _vp, _vp]),
+    "vpmc_advect": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i]),
     "vpmc_sim_set_law": (_i, [_vp, _i]),
     "vpmc_sim_set_seed": (_i, [_vp, _u64]),
     "vpmc_sim_set_step": (_i, [_vp, _u64]),

@@ -90,8 +90,9 @@ def build_cpp_check(force: bool = False) -> str:
     if not force and os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
         return out
     cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
-    cmd = ["g++", "-std=c++20", "-O2", "-I", INCLUDE, "-I", cuda_inc, src, "-o", out, "-L", PKG, "-lvpmc",
-           f"-Wl,-rpath,{PKG}"]
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+    cmd = ["g++", "-std=c++20", "-O2", "-Wall", "-I", INCLUDE, "-I", cuda_inc, src, "-o", out, "-L", PKG, "-lvpmc",
+           f"-Wl,-rpath,{PKG}", "-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{cuda_lib}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"g++ failed:\n$ {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

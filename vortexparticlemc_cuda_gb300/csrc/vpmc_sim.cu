@@ -313,6 +313,29 @@ __global__ void k_taylor_green(const float2* __restrict__ pos, long n, double* _
     }
 }
 
+__global__ void k_advect(float2* __restrict__ pos, const float2* __restrict__ vel, const double* __restrict__ vel64,
+                         long n, float dt, float Lx, float Ly, int periodic) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const float2 x = pos[i];
+        const double vx = vel64 ? vel64[2 * i] : double(vel[i].x);
+        const double vy = vel64 ? vel64[2 * i + 1] : double(vel[i].y);
+        double nx = double(x.x) + double(dt) * vx, ny = double(x.y) + double(dt) * vy;
+        float ox, oy;
+        if (periodic) {
+            nx -= floor(nx / double(Lx)) * double(Lx);
+            ny -= floor(ny / double(Ly)) * double(Ly);
+            ox = float(nx);
+            oy = float(ny);
+            if (ox >= Lx) ox = 0.f;
+            if (oy >= Ly) oy = 0.f;
+        } else {
+            ox = float(nx);
+            oy = float(ny);
+        }
+        pos[i] = make_float2(ox, oy);
+    }
+}
+
 __global__ void k_check_finite(const float2* __restrict__ p, long n, unsigned* flags) {
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
         const float2 v = p[i];
@@ -668,6 +691,16 @@ int vpmc_sim_destroy(vpmc_sim* s) {
 }
 
 int vpmc_sim_num_particles(vpmc_sim* s) { return s ? int(s->N) : -1; }
+
+int vpmc_advect(vpmc_context* ctx, int N, float* pos, const float* vel, const double* vel64, float dt, float Lx,
+                float Ly, int periodic) {
+    if (!ctx || N < 0 || (N > 0 && (!pos || (!vel && !vel64))) || !(Lx > 0.f) || !(Ly > 0.f)) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    if (N > 0)
+        VPMC_LAUNCH(k_advect, blocks_for(N), 256, 0, ctx->stream, reinterpret_cast<float2*>(pos),
+                    reinterpret_cast<const float2*>(vel), vel64, long(N), dt, Lx, Ly, periodic);
+    return vpmc_context_sync(ctx);
+}
 
 int vpmc_sim_set_particles(vpmc_sim* s, const float* pos, const float* omega, int is_host) {
     if (!s) return VPMC_ERR_INVALID;
