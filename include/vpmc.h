@@ -276,6 +276,14 @@ int vpmc_sim_set_seed(vpmc_sim* sim, uint64_t seed);
 int vpmc_sim_set_step(vpmc_sim* sim, uint64_t step);
 uint64_t vpmc_sim_get_step(vpmc_sim* sim);
 
+/* Arithmetic of the MIS step: 32 (default: FP32 pair arithmetic with
+ * compensated sums) or 64 (the plain FP64 path of the same estimator: field
+ * values, MIS terms, sums and the Euler update in FP64; sample points are
+ * drawn as in FP32 mode).  The FP64 path exists as the comparison baseline
+ * north of which the FP32 path is measured; on GB300 FP64 runs at a small
+ * fraction of the FP32 rate. */
+int vpmc_sim_set_precision(vpmc_sim* sim, int bits);
+
 /* Neighbour-walk tuning: cells per h_w (k >= 1, walk (2k+1)^2 cells) and
  * queries per thread in the field-evaluation kernel (4 or 8).  0 = auto. */
 int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);

@@ -164,6 +164,21 @@ def test_autotune_picks_a_candidate_and_caches(cuda):
     assert sim2.autotune() == (k, q, -1.0)     # cached by shape
 
 
+@pytest.mark.parametrize("law", [0, 1])
+def test_fp64_path_matches_fp32_path(cuda, law):
+    """The plain FP64 path of the same estimator draws the same samples; its
+    velocities agree with the FP32 path to FP32 rounding of the field sums."""
+    sim, pos, om, prm = _setup(cuda, law=law)
+    v32 = sim.velocity(step=3).cpu().numpy()
+    sim.set_precision(64)
+    v64 = sim.velocity(step=3).cpu().numpy()
+    assert np.isfinite(v64).all()
+    rel = np.abs(v64 - v32).max() / np.abs(v64).max()
+    assert rel < 2e-4, rel
+    sim.set_precision(32)
+    assert np.array_equal(sim.velocity(step=3).cpu().numpy(), v32)
+
+
 def test_empty_sign_subset(cuda):
     """All strengths positive: the negative branch contributes nothing (the
     reference would index sub[-1])."""

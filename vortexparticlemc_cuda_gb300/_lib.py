@@ -79,6 +79,7 @@ SIGNATURES = {
     "vpmc_sim_set_step": (_i, [_vp, _u64]),
     "vpmc_sim_get_step": (_u64, [_vp]),
     "vpmc_sim_set_tuning": (_i, [_vp, _i, _i]),
+    "vpmc_sim_set_precision": (_i, [_vp, _i]),
     "vpmc_sim_get_tuning": (_i, [_vp, _vp, _vp]),
     "vpmc_sim_autotune": (_i, [_vp, _vp, _vp, _vp]),
     "vpmc_sim_last_stats": (_i, [_vp, _vp, _vp]),

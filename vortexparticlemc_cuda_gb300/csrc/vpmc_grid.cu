@@ -75,8 +75,10 @@ __global__ void k_grid_gather(const uint32_t* __restrict__ perm, const uint32_t*
         float2 q = pos[i];
         if (G.periodic) { q.x = wrapf(q.x, G.Lx); q.y = wrapf(q.y, G.Ly); }
         const float w = omega ? omega[i] : 1.f;
-        const float wt = (set_mode == SET_ONE_SIGNED ? w : fabsf(w)) * G.two_sigma;
-        cand[p] = Cand{q.x, q.x, q.y, q.y, wt, wt, 0.f, 0.f};
+        // weight 2 sigma |omega| (or 2 sigma omega), FP32 hi part + remainder
+        const double wd = double(set_mode == SET_ONE_SIGNED ? w : fabsf(w)) * (80.0 / (7.0 * kPiD * double(G.hw) * G.hw));
+        const float wt = float(wd);
+        cand[p] = Cand{q.x, q.x, q.y, q.y, wt, wt, float(wd - double(wt)), 0.f};
     }
 }
 
@@ -273,10 +275,11 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
+    constexpr bool kField64 = MODE == EVAL_FIELD64 || MODE == EVAL_FIELD9_64;
     constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9;
     constexpr int NP = QPT / 2;   // packed query pairs
     static_assert(!kPacked || (QPT % 2 == 0), "packed path needs an even query count");
-    using Acc = typename std::conditional<kF64, double, float>::type;
+    using Acc = typename std::conditional<kF64 || kField64, double, float>::type;
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -440,6 +443,31 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                         part[2 * pr] = lo;
                         part[2 * pr + 1] = hi;
                     }
+                } else if constexpr (kField64) {
+                    // the plain FP64 path: every pair and the sum in FP64
+                    const double hw = double(G.hw), ih = 1.0 / hw;
+                    const double A = 3.0 * ih * ih * ih, B = -3.0 * ih * ih;
+                    double px[QPT], py[QPT];
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        px[j] = double(qx[j]) + double(pc.qdx);
+                        py[j] = double(qy[j]) + double(pc.qdy);
+                        part[j] = 0.0;
+                    }
+                    for (int c = 0; c < cnt; ++c) {
+                        const Cand cv = cs[c];
+                        const double cxd = cv.x, cyd = cv.y, wd = double(cv.w) + double(cv.wl);
+#pragma unroll
+                        for (int j = 0; j < QPT; ++j) {
+                            const double dx = cxd - px[j], dy = cyd - py[j];
+                            const double r2 = dx * dx + dy * dy;
+                            const double r = sqrt(r2);
+                            const double inner = 0.5 + r2 * (A * r + B);
+                            const double t = 1.0 - ih * r;
+                            const double v = fmax(fmin(inner, t * t * t), 0.0);
+                            part[j] += wd * v;
+                        }
+                    }
                 } else if constexpr (kF64) {
                     float px[QPT], py[QPT];
 #pragma unroll
@@ -492,7 +520,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 #pragma unroll
                 for (int j = 0; j < QPT; ++j) {
                     bool use = true;
-                    if (MODE == EVAL_FIELD9) {
+                    if (MODE == EVAL_FIELD9 || MODE == EVAL_FIELD9_64) {
                         const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
                         use = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
                     }
@@ -515,7 +543,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 #pragma unroll
         for (int j = 0; j < QPT; ++j) {
             if (!qv[j]) continue;
-            if constexpr (kF64) a.out_f64[qid[j]] = acc[j];
+            if constexpr (kF64 || kField64) a.out_f64[qid[j]] = acc[j];
             else if constexpr (kComp) a.out_f64[qid[j]] = double(acc[j]) - double(acc_c[j]);
             else a.out_f32[qid[j]] = acc[j];
         }
@@ -698,6 +726,8 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
         case EVAL_SPMV32:
             if (L.qpt != 4) return VPMC_ERR_INVALID;
             return launch_eval_t<EVAL_SPMV32, 4>(ctx, a);
+        case EVAL_FIELD64: return launch_eval_t<EVAL_FIELD64, 4>(ctx, a);
+        case EVAL_FIELD9_64: return launch_eval_t<EVAL_FIELD9_64, 4>(ctx, a);
         default: return VPMC_ERR_INVALID;
     }
 }

@@ -62,6 +62,8 @@ enum EvalMode : int {
     EVAL_FIELD_EXC = 2,  // as FIELD, pairs closer than 1e-6 skipped (exclude_center)
     EVAL_SPMV64 = 3,     // out_f64[id] = sum (w + w_lo) W, in-support pairs in FP64
     EVAL_SPMV32 = 4,     // out_f64[id] = compensated FP32 sum
+    EVAL_FIELD64 = 5,    // as FIELD, every pair in FP64 (weight w + wl), out_f64[id]
+    EVAL_FIELD9_64 = 6,  // as FIELD9 in FP64
 };
 
 enum SetMode : int {

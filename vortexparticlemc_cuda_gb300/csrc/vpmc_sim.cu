@@ -300,6 +300,102 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
     }
 }
 
+// The plain FP64 path of the same estimator: field values, MIS terms, sums
+// and the Euler update in FP64 (sample points are drawn as in FP32 mode).
+__device__ __forceinline__ double2 mis_term64(int law, float2 xf, float2 yf, double f, double w1, double w2,
+                                              double cum, double alpha, double R, const InstMC& I) {
+    if (!(f > 0.0)) return make_double2(0.0, 0.0);
+    const double rx = double(xf.x) - double(yf.x), ry = double(xf.y) - double(yf.y);
+    if (law == VPMC_LAW_REFERENCE) {
+        double wx = rx, wy = ry;
+        if (I.periodic) {
+            wx = rx - round(rx / I.Lx) * I.Lx;
+            wy = ry - round(ry / I.Ly) * I.Ly;
+        }
+        const double rn = fmax(sqrt(wx * wx + wy * wy), 1e-6);
+        const double inv_r2 = 1.0 / (rx * rx + ry * ry + 1e-8);
+        const double denom = w1 * f / cum + w2 * alpha / rn;
+        const double sc = f / denom * inv_r2 / (2.0 * kPiD);
+        return make_double2(-ry * sc, rx * sc);
+    }
+    const double r2 = rx * rx + ry * ry;
+    if (!(r2 > 0.0)) return make_double2(0.0, 0.0);
+    const double rn = sqrt(r2);
+    const double p2 = rn < R ? alpha / rn : 0.0;
+    const double sc = f / ((w1 * f / cum + w2 * p2) * (2.0 * kPiD * r2));
+    return make_double2(-ry * sc, rx * sc);
+}
+
+struct AccArgs64 {
+    const InstMC* mc;
+    int n_inst;
+    const float2* pos;
+    const float2* ys;
+    const double* fv;
+    const double* cum64;   // per instance: Omega_+, Omega_- (x9 when periodic), FP64
+    long t0, nt;
+    int N1, N2;
+    int advect;
+    float2* vel;
+    float2* pos_out;
+};
+
+__global__ void __launch_bounds__(256) k_accum64(AccArgs64 a) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
+    const int Q = a.N1 + a.N2;
+    const double w1 = double(a.N1) / Q, w2 = double(a.N2) / Q;
+    for (long tl = warp; tl < a.nt; tl += nwarps) {
+        const long t = a.t0 + tl;
+        const int ii = inst_of(a.mc, a.n_inst, t);
+        const InstMC& I = a.mc[ii];
+        const float2 x = a.pos[t];
+        const double R = sqrt(double(I.Lx) * I.Lx + double(I.Ly) * I.Ly);
+        const double alpha = 1.0 / (2.0 * kPiD * R);
+        double u[2][2];
+        for (int s = 0; s < 2; ++s) {
+            double sx = 0.0, sy = 0.0;
+            const long base = (tl * 2 + s) * Q;
+            for (int j = lane; j < Q; j += 32) {
+                const double2 c = mis_term64(I.law, x, a.ys[base + j], a.fv[base + j], w1, w2, a.cum64[2 * ii + s],
+                                             alpha, R, I);
+                sx += c.x;
+                sy += c.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {   // fixed butterfly, identical on every lane
+                const double ox = __shfl_xor_sync(0xffffffffu, sx, o), oy = __shfl_xor_sync(0xffffffffu, sy, o);
+                const bool lo = (lane & o) == 0;
+                sx = lo ? sx + ox : ox + sx;
+                sy = lo ? sy + oy : oy + sy;
+            }
+            u[s][0] = sx / Q;
+            u[s][1] = sy / Q;
+        }
+        if (lane == 0) {
+            const double vx = u[0][0] - u[1][0], vy = u[0][1] - u[1][1];
+            a.vel[t] = make_float2(float(vx), float(vy));
+            if (a.advect) {
+                double nx = double(x.x) + double(I.dt) * vx, ny = double(x.y) + double(I.dt) * vy;
+                float ox, oy;
+                if (I.periodic) {
+                    nx -= floor(nx / double(I.Lx)) * double(I.Lx);
+                    ny -= floor(ny / double(I.Ly)) * double(I.Ly);
+                    ox = float(nx);
+                    oy = float(ny);
+                    if (ox >= I.Lx) ox = 0.f;
+                    if (oy >= I.Ly) oy = 0.f;
+                } else {
+                    ox = float(nx);
+                    oy = float(ny);
+                }
+                a.pos_out[t] = make_float2(ox, oy);
+            }
+        }
+    }
+}
+
 __global__ void k_inc_step(unsigned long long* s) { *s += 1ull; }
 
 // taylor_green_vorticity (include/analytical_flow.hpp:24-28) evaluated in
@@ -405,6 +501,9 @@ struct vpmc_sim {
     QueryBufs q;
     float2* ys = nullptr;
     float* fv = nullptr;
+    double* fv64 = nullptr;            // FP64 path only
+    double* cum64 = nullptr;           // per instance Omega_+-, x9 when periodic (FP64 path)
+    int precision = 32;
     long chunk_targets = 0;
     long max_samples = 0;
     // graphs
@@ -477,6 +576,8 @@ int alloc_work(vpmc_sim* s) {
         carve_queries(c, nb, ns, &s->q);
         s->ys = c.take<float2>(size_t(ns));
         s->fv = c.take<float>(size_t(ns));
+        s->fv64 = s->precision == 64 ? c.take<double>(size_t(ns)) : nullptr;
+        s->cum64 = c.take<double>(2 * size_t(s->n_inst));
     };
     Carver dry;
     carve_all(dry);
@@ -511,19 +612,29 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
                    nt, s->N1, s->N2, s->ys, s->q.qbin, s->q.qcount};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
         VPMC_TRY(scatter_points(ctx, s->g, s->q, s->ys, ns, 0));
-        VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->qpt)));
-        VPMC_CUDA(cudaMemsetAsync(s->fv, 0, sizeof(float) * size_t(ns), st));
+        VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->precision == 64 ? 4 : s->qpt)));
+        const bool f64 = s->precision == 64;
+        if (f64) VPMC_CUDA(cudaMemsetAsync(s->fv64, 0, sizeof(double) * size_t(ns), st));
+        else VPMC_CUDA(cudaMemsetAsync(s->fv, 0, sizeof(float) * size_t(ns), st));
         EvalLaunch L;
-        L.mode = s->mc[0].law == VPMC_LAW_UNBIASED ? EVAL_FIELD9 : EVAL_FIELD;
-        L.qpt = s->qpt;
+        const bool unb = s->mc[0].law == VPMC_LAW_UNBIASED;
+        L.mode = f64 ? (unb ? EVAL_FIELD9_64 : EVAL_FIELD64) : (unb ? EVAL_FIELD9 : EVAL_FIELD);
+        L.qpt = f64 ? 4 : s->qpt;
         L.out_f32 = s->fv;
+        L.out_f64 = s->fv64;
         const size_t ci = size_t(t0 / s->chunk_targets);
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, ev_flags));
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, ev_flags));
-        AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
-                   s->pos_next};
-        VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
+        if (f64) {
+            AccArgs64 aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv64, s->cum64, t0, nt, s->N1, s->N2, advect ? 1 : 0,
+                         s->vel, s->pos_next};
+            VPMC_LAUNCH(k_accum64, blocks_for(nt * 32), 256, 0, st, aa);
+        } else {
+            AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
+                       s->pos_next};
+            VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
+        }
     }
     if (advect) {
         VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
@@ -735,6 +846,7 @@ int vpmc_sim_prepare(vpmc_sim* s) {
     VPMC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     long goff = 0;
+    std::vector<double> cum64_h;
     for (int i = 0; i < s->n_inst; ++i) {
         const long b = s->begin[i], n = s->counts[i];
         InstMC& m = s->mc[i];
@@ -750,6 +862,8 @@ int vpmc_sim_prepare(vpmc_sim* s) {
         const float f9 = m.periodic ? 9.f : 1.f;
         m.cum9[0] = float(cum[0]) * f9;
         m.cum9[1] = float(cum[1]) * f9;
+        cum64_h.push_back(cum[0] * (m.periodic ? 9.0 : 1.0));
+        cum64_h.push_back(cum[1] * (m.periodic ? 9.0 : 1.0));
         for (int sg = 0; sg < 2; ++sg) {
             m.goff[sg] = goff;
             if (cnt[sg] > 0)
@@ -758,6 +872,7 @@ int vpmc_sim_prepare(vpmc_sim* s) {
         }
     }
     VPMC_TRY(upload_mc(s));
+    VPMC_CUDA(cudaMemcpyAsync(s->cum64, cum64_h.data(), sizeof(double) * cum64_h.size(), cudaMemcpyHostToDevice, st));
     VPMC_CUDA(cudaStreamSynchronize(st));
     drop_graphs(s);
     s->prepared = true;
@@ -855,6 +970,18 @@ int vpmc_sim_set_step(vpmc_sim* s, uint64_t step) {
 }
 
 uint64_t vpmc_sim_get_step(vpmc_sim* s) { return s ? s->step : 0; }
+
+int vpmc_sim_set_precision(vpmc_sim* s, int bits) {
+    if (!s || (bits != 32 && bits != 64)) return VPMC_ERR_INVALID;
+    if (bits == s->precision) return VPMC_OK;
+    s->precision = bits;
+    VPMC_TRY(alloc_work(s));
+    if (s->prepared) {   // the FP64 totals live in the re-carved working set
+        s->prepared = false;
+        VPMC_TRY(vpmc_sim_prepare(s));
+    }
+    return vpmc_context_sync(s->ctx);
+}
 
 int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
     if (!s || k_walk < 0 || k_walk > 4 || !(qpt == 0 || qpt == 4 || qpt == 8)) return VPMC_ERR_INVALID;

@@ -350,6 +350,10 @@ class Simulation:
     def step_count(self) -> int:
         return int(lib().vpmc_sim_get_step(self.h))
 
+    def set_precision(self, bits: int):
+        """32: FP32 pair arithmetic + compensated sums; 64: the plain FP64 path."""
+        check(lib().vpmc_sim_set_precision(self.h, int(bits)), "vpmc_sim_set_precision")
+
     def set_tuning(self, k_walk: int = 0, queries_per_thread: int = 0):
         check(lib().vpmc_sim_set_tuning(self.h, int(k_walk), int(queries_per_thread)), "vpmc_sim_set_tuning")
 
