@@ -138,6 +138,27 @@ __global__ void k_scatter_points(const float2* __restrict__ pts, long M, const G
     }
 }
 
+// Scatter with precomputed in-bin ranks: slot = qstart[bin] + rank.
+__global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const GridInst* __restrict__ inst,
+                                 int n_inst, const uint32_t* __restrict__ qbin, const uint32_t* __restrict__ qrank,
+                                 const uint32_t* __restrict__ qstart, QRec* __restrict__ qrec) {
+    for (long m = long(blockIdx.x) * blockDim.x + threadIdx.x; m < M; m += long(gridDim.x) * blockDim.x) {
+        const uint32_t b = qbin[m];
+        if (b == kNoBin) continue;
+        const GridInst& G = inst[inst_of_bin(inst, n_inst, b)];
+        float2 p = pts[m];
+        uint32_t fl = (2u) | (2u << 3);
+        if (G.periodic) {
+            const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+            p.x = p.x - kx * G.Lx;
+            p.y = p.y - ky * G.Ly;
+            const int ikx = min(max(int(kx), -2), 2), iky = min(max(int(ky), -2), 2);
+            fl = uint32_t(ikx + 2) | (uint32_t(iky + 2) << 3);
+        }
+        qrec[qstart[b] + qrank[m]] = QRec{p.x, p.y, uint32_t(m), fl};
+    }
+}
+
 __global__ void k_items_count(const uint32_t* __restrict__ qstart, long nbins, int chunk,
                               uint32_t* __restrict__ per_bin) {
     for (long b = long(blockIdx.x) * blockDim.x + threadIdx.x; b < nbins; b += long(gridDim.x) * blockDim.x) {
@@ -229,7 +250,7 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 // Sum over one staged run of candidates for NPR packed query pairs, in
 // bin-local coordinates: candidates hold (x, y) relative to the bin centre
 // and c2 = x^2 + y^2; queries enter as -2 q and |q|^2, so
-//   r^2 = max(c2 + q2 - 2 c.q, 0),  r = sqrt(r^2)
+//   r^2 = c2 + q2 - 2 c.q,  r = sqrt(|r^2|)
 //   P  += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)      (= w W / 2 sigma)
 // 9 FMA-pipe operations per pair (2 per query of r^2 setup, 1 sqrt on the XU).
 template <int NPR, int NPMAX>
@@ -248,11 +269,10 @@ __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt,
             const f2x r2p = fma2(XY.y, QY[pr], fma2(XY.x, QX[pr], s));
             float ra, rb;
             up2(r2p, ra, rb);
-            ra = fmaxf(ra, 0.f);
-            rb = fmaxf(rb, 0.f);
-            const f2x r2 = pk2(ra, rb);
-            const f2x r = pk2(sqrt_approx(ra), sqrt_approx(rb));
-            const f2x in = fma2(r2, fma2(A2, r, B2), HALF);
+            // rounding can leave r^2 a hair below 0 when c ~ q: take sqrt(|r^2|);
+            // the polynomial's r^2 term is then off by that hair only
+            const f2x r = pk2(sqrt_approx(fabsf(ra)), sqrt_approx(fabsf(rb)));
+            const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
             const f2x t = fma2(NIH, r, ONE);
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
@@ -687,6 +707,7 @@ void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q) {
     q->qcount = c.take<uint32_t>(size_t(nbins + 1));
     q->qstart = c.take<uint32_t>(size_t(nbins + 1));
     q->qfill = c.take<uint32_t>(size_t(nbins + 1));
+    q->qrank = c.take<uint32_t>(m);
     q->qrec = c.take<QRec>(m);
     q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
 }
@@ -698,6 +719,13 @@ int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
     VPMC_CUDA(cudaMemsetAsync(q.qfill, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
     VPMC_LAUNCH(k_scatter_points, blocks_for(M), 256, 0, st, pts, M, g.inst, g.n_inst, q.qbin, q.qstart, q.qfill,
                 q.qrec);
+    return VPMC_OK;
+}
+
+int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M) {
+    VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
+    VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, ctx->stream, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,
+                q.qstart, q.qrec);
     return VPMC_OK;
 }
 

@@ -133,6 +133,7 @@ struct QueryBufs {
     uint32_t* qcount = nullptr;  // nbins + 1
     uint32_t* qstart = nullptr;  // nbins + 1
     uint32_t* qfill = nullptr;   // nbins
+    uint32_t* qrank = nullptr;   // per point: rank inside its bin (from the counting atomic)
     QRec* qrec = nullptr;        // max points
     uint32_t* scan_tmp = nullptr;
 };
@@ -144,6 +145,8 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 // Scatter points whose bins are already in q.qbin (counts in q.qcount).
 int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M,
                    int field9);
+// Same, with each point's rank inside its bin already in q.qrank (no atomics).
+int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M);
 
 struct EvalLaunch {
     int mode = EVAL_FIELD;

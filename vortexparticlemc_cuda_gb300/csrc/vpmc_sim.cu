@@ -118,6 +118,7 @@ struct GenArgs {
     float2* ys;
     uint32_t* qbin;
     uint32_t* qcount;
+    uint32_t* qrank;
 };
 
 __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
@@ -199,7 +200,8 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                 const int cx = min(max(floor_int(px * G.inv_sx), 0), G.gx - 1);
                 const int cy = min(max(floor_int(py * G.inv_sy), 0), G.gy - 1);
                 b = uint32_t(G.bin_base) + uint32_t(s) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
-                atomicAdd(&a.qcount[b], 1u);
+                // the counting atomic also hands out this sample's slot in its bin
+                a.qrank[sid] = atomicAdd(&a.qcount[b], 1u);
             }
         }
         a.ys[sid] = y;
@@ -609,9 +611,9 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
         GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
-                   nt, s->N1, s->N2, s->ys, s->q.qbin, s->q.qcount};
+                   nt, s->N1, s->N2, s->ys, s->q.qbin, s->q.qcount, s->q.qrank};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
-        VPMC_TRY(scatter_points(ctx, s->g, s->q, s->ys, ns, 0));
+        VPMC_TRY(scatter_ranked(ctx, s->g, s->q, s->ys, ns));
         VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->precision == 64 ? 4 : s->qpt)));
         const bool f64 = s->precision == 64;
         if (f64) VPMC_CUDA(cudaMemsetAsync(s->fv64, 0, sizeof(double) * size_t(ns), st));
