@@ -114,6 +114,28 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """Largest x over the ranks of the default process group (x itself
+    without one): the replica timing takes the slowest rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, world: int, steps: int, ms_max: float) -> float:
+    """Whole-job units/s of `world` independent replicas timed by the slowest."""
+    return units_per_rank * world * steps / (ms_max / 1e3)
+
+
+def reports(rank: int) -> bool:
+    """Only rank 0 prints the JSON line (and runs the CPU reference arm)."""
+    return rank == 0
+
+
 def profile_traffic(workload: str):
     """DRAM bytes per eval launch from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", f"k_eval_{workload}.md")
@@ -172,7 +194,7 @@ def strengths_cpu(wl, pos, b):
 def run_reference(args, wl):
     import oracle as O
     rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if not reports(rank):
         return 0
     pos = O.lattice(wl["Nx"])
     b = O.taylor_green(pos)
@@ -285,11 +307,8 @@ def run_gpu(args, wl):
     ms = e0.elapsed_time(e1)
     log(f"timed {args.steps} steps: {ms / args.steps:.1f} ms/step, eval {np.mean(eval_ms):.1f} ms/step")
     stats = sim.last_stats()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = N * world * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ms, dev)
+    value = replica_throughput(N, world, args.steps, ms)
 
     # end to end through the host-buffer C-ABI call
     pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
@@ -305,7 +324,8 @@ def run_gpu(args, wl):
         a_in, a_out = a_out, a_in
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": N * world * args.e2e_steps / e2e_s, "unit": "particle-steps/s",
+    e2e_ms = max_over_ranks(1e3 * e2e_s, dev)
+    e2e = {"value": replica_throughput(N, world, args.e2e_steps, e2e_ms), "unit": "particle-steps/s",
            "h2d_bytes_per_step": int(pos.nbytes), "d2h_bytes_per_step": int(2 * pos.nbytes),
            "steps": args.e2e_steps, "call": "vpmc_sim_step_host (pinned host buffers)"}
 
@@ -358,7 +378,7 @@ def run_gpu(args, wl):
         "cg": {**cg, "seconds": t_cg},
         "autotune": tune,
     }
-    if rank == 0:
+    if reports(rank):
         print(json.dumps(out))
     sim.close()
     if world > 1:

@@ -2,8 +2,8 @@
 // (include/vortex_particle_mc.hpp:16-209): SimParam, ParticleSet,
 // VorticityView, Simulation.  Header-only; every method forwards to the C ABI
 // in vpmc.h (GPU only).  Differences from the reference, by design:
-//   * step_cuda runs the plain path (auxiliary points off, F = I); the
-//     5-point kernel deformation is not in this build;
+//   * step_cuda runs the reference's deformation step (aux = 1, F update)
+//     by default; set_deformation(false) selects the plain method;
 //   * the estimator law defaults to the reference kernel's sampling law and
 //     can be switched to the unbiased law (set_law);
 //   * the *_cpu members throw vpmc::unsupported.
@@ -209,8 +209,10 @@ public:
     std::mt19937 rng;
     void step_cpu(bool) { throw vpmc::unsupported("Simulation::step_cpu"); }
 
-    // step_cuda (src/cuda/simulation_step.cu:9-90), plain path: MIS velocity of
-    // every particle, x += dt u, periodic wrap in FP64.
+    // step_cuda (src/cuda/simulation_step.cu:9-90): MIS velocity of every
+    // particle with deformed kernels and the four auxiliary points, F =
+    // renorm_det1(I + dt grad u), x += dt u with the periodic wrap in FP64.
+    // With set_deformation(false): the plain method (F unused).
     void step_cuda(bool periodic) {
         ensure_sim(periodic);
         vpmc::check(vpmc_sim_set_particles(sim_, reinterpret_cast<const float*>(particles_.d_p()),
@@ -218,30 +220,42 @@ public:
                     "step_cuda: set particles");
         if (omega_dirty_) vpmc::check(vpmc_sim_prepare(sim_), "step_cuda: prepare");
         omega_dirty_ = false;
+        if (deformation_ != sim_deform_) {
+            vpmc::check(vpmc_sim_set_deformation(sim_, deformation_ ? 1 : 0, 0.f), "step_cuda: deformation");
+            sim_deform_ = deformation_;
+        }
+        if (deformation_)
+            vpmc::check(vpmc_sim_set_F(sim_, reinterpret_cast<const float*>(particles_.d_F()), 0), "step_cuda: F");
         vpmc::check(vpmc_sim_step(sim_, 1, 1), "step_cuda");
         vpmc::check(vpmc_sim_get_particles(sim_, reinterpret_cast<float*>(particles_.d_p()), nullptr,
                                            reinterpret_cast<float*>(particles_.d_v()), 0),
                     "step_cuda: get particles");
+        if (deformation_)
+            vpmc::check(vpmc_sim_get_F(sim_, reinterpret_cast<float*>(particles_.d_F()), 0), "step_cuda: F out");
     }
 
     // compute_velocity_naive (src/cuda/simulation_step.cu:92-108): Plummer
-    // minimum-image direct sum, here in FP64.
+    // minimum-image direct sum in FP32 (the reference's kernel is FP32), written
+    // to particles.vel.  compute_velocity_naive_f64 gives the FP64 sum.
     void compute_velocity_naive(bool periodic, float eps_core) {
         const int N = particles_.N_cur;
-        dvec<double> uv(size_t(2) * std::max(N, 1));
-        direct_plummer(periodic, eps_core, uv);
-        std::vector<double> h = uv.to_host();
-        std::vector<float2> v(particles_.vel.size(), float2{0.f, 0.f});
-        for (int i = 0; i < N; ++i) v[i] = float2{float(h[2 * i]), float(h[2 * i + 1])};
-        particles_.vel.assign(v);
+        if (particles_.vel.size() < size_t(N)) particles_.vel.resize(N);
+        direct_plummer_f32(periodic, eps_core, reinterpret_cast<float*>(particles_.d_v()));
     }
 
+    void compute_velocity_naive_f64(bool periodic, float eps_core, dvec<double>& uv) {
+        uv.resize(size_t(2) * std::max(particles_.N_cur, 1));
+        direct_plummer(periodic, eps_core, uv);
+    }
+
+    // step_cuda_naive (src/cuda/simulation_step.cu:110-129): eps = h_w/2, FP32
+    // velocities, forward Euler, periodic wrap.
     void step_cuda_naive(bool periodic) {
         const int N = particles_.N_cur;
-        dvec<double> uv(size_t(2) * std::max(N, 1));
-        direct_plummer(periodic, 0.5f * P_.h_w, uv);
-        vpmc::check(vpmc_advect(ctx(), N, reinterpret_cast<float*>(particles_.d_p()), nullptr, raw_ptr(uv), P_.dt,
-                                P_.Lx, P_.Ly, periodic ? 1 : 0),
+        compute_velocity_naive(periodic, 0.5f * P_.h_w);
+        vpmc::check(vpmc_advect(ctx(), N, reinterpret_cast<float*>(particles_.d_p()),
+                                reinterpret_cast<const float*>(particles_.d_v()), nullptr, P_.dt, P_.Lx, P_.Ly,
+                                periodic ? 1 : 0),
                     "step_cuda_naive");
     }
 
@@ -317,6 +331,35 @@ public:
         law_ = law;
         if (sim_) vpmc::check(vpmc_sim_set_law(sim_, law), "set_law");
     }
+    // step_cuda with (default, as the reference) or without the 5-point deformation.
+    void set_deformation(bool on) { deformation_ = on; }
+    // Reinitialisation (the reference's README describes it; its code has
+    // none): positions to the lattice, F = I, strengths re-fitted by CG-RBF to
+    // the current field.  Returns {iters, relres, true relres}.
+    std::vector<double> reinitialize(double tol, int max_iter, bool periodic = true) {
+        ensure_sim(periodic);
+        vpmc::check(vpmc_sim_set_particles(sim_, reinterpret_cast<const float*>(particles_.d_p()),
+                                           particles_.d_omega(), 0),
+                    "reinitialize: set particles");
+        if (deformation_ != sim_deform_) {
+            vpmc::check(vpmc_sim_set_deformation(sim_, deformation_ ? 1 : 0, 0.f), "reinitialize: deformation");
+            sim_deform_ = deformation_;
+        }
+        if (deformation_)
+            vpmc::check(vpmc_sim_set_F(sim_, reinterpret_cast<const float*>(particles_.d_F()), 0), "reinitialize: F");
+        std::vector<double> info(3, 0.0);
+        const int rc = vpmc_sim_reinit(sim_, tol, max_iter, info.data());
+        if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) vpmc::check(rc, "reinitialize");
+        vpmc::check(vpmc_sim_get_particles(sim_, reinterpret_cast<float*>(particles_.d_p()), particles_.d_omega(),
+                                           nullptr, 0),
+                    "reinitialize: get particles");
+        vpmc::check(vpmc_sim_get_F(sim_, reinterpret_cast<float*>(particles_.d_F()), 0), "reinitialize: F out");
+        // the reference-shaped subsets and hashes follow the new state
+        build_subsets_cuda();
+        do_spatial_hashing();
+        build_global_hash();
+        return info;
+    }
     // CG with explicit tolerance (conjugate_gradient_rbf uses the reference defaults).
     std::vector<double> conjugate_gradient(double tol, int max_iter) {
         std::vector<double> info(3, 0.0);
@@ -363,6 +406,7 @@ private:
         const int n = particles_.N_cur;
         vpmc::check(vpmc_sim_create(ctx(), 1, &p, &n, &sim_), "vpmc_sim_create");
         sim_periodic_ = periodic;
+        sim_deform_ = false;
         omega_dirty_ = true;
     }
 
@@ -377,6 +421,18 @@ private:
                                              N, nullptr, raw_ptr(tidx), eps, P_.Lx, P_.Ly, periodic ? 1 : 0,
                                              raw_ptr(uv)),
                     "direct Biot-Savart");
+    }
+
+    void direct_plummer_f32(bool periodic, float eps, float* out) {
+        const int N = particles_.N_cur;
+        std::vector<int> iota(N);
+        std::iota(iota.begin(), iota.end(), 0);
+        dvec<int> tidx;
+        tidx.assign(iota);
+        vpmc::check(vpmc_direct_velocity_f32(ctx(), VPMC_DIRECT_PLUMMER, N,
+                                             reinterpret_cast<const float*>(particles_.d_p()), particles_.d_omega(),
+                                             N, nullptr, raw_ptr(tidx), eps, P_.Lx, P_.Ly, periodic ? 1 : 0, out),
+                    "direct Biot-Savart (FP32)");
     }
 
     SpatialHash hash_pos_, hash_neg_, hash_all_;
@@ -394,6 +450,8 @@ private:
 
     vpmc_sim* sim_ = nullptr;
     bool sim_periodic_ = true;
+    bool deformation_ = true;
+    bool sim_deform_ = false;
     bool omega_dirty_ = true;
     int law_ = VPMC_LAW_REFERENCE;
 };

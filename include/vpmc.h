@@ -204,6 +204,14 @@ int vpmc_direct_velocity_f64(vpmc_context* ctx, int kernel, int N, const float* 
                              double param, double Lx, double Ly, int periodic,
                              double* out_uv);
 
+/* The same direct sums in FP32 tiles: the deterministic "P" particle method
+ * of the reference (biot_savart_naive_kernel is FP32), for P-vs-MC
+ * comparisons.  param = eps (Plummer) or h_w (mollified); out_uv: 2*M floats
+ * (device).  Fixed-order sums (deterministic). */
+int vpmc_direct_velocity_f32(vpmc_context* ctx, int kernel, int N, const float* pos,
+                             const float* omega, int M, const float* pts, const int* tidx,
+                             float param, float Lx, float Ly, int periodic, float* out_uv);
+
 /* ------------------------------------------------- simulation (a8, a9, a12)
  * SimParam, include/vortex_particle_mc.hpp:96-134; one entry per instance.
  * h = Lx/Nx, h_w = h*hwr, dx = h_w/2 are derived as the reference does.  */
@@ -269,6 +277,48 @@ int vpmc_sim_step_host(vpmc_sim* sim, const float* pos_in, float* pos_out, float
  * vel64 (double2).  Device pointers. */
 int vpmc_advect(vpmc_context* ctx, int N, float* pos, const float* vel, const double* vel64, float dt,
                 float Lx, float Ly, int periodic);
+
+/* Deformation mode (the reference's Simulation::step_cuda, src/cuda/
+ * simulation_step.cu:9-90, which runs monte_carlo_bs_kernel_safe with aux = 1
+ * and update_jacobian_from5): each particle carries F (row-major
+ * {F11, F12, F21, F22}, identity at creation); vorticity kernels become
+ * W(|F^-1 d|), branch-1 jitter becomes F r, every target gets the four
+ * auxiliary points x -/+ dx e_x, x +/- dx e_y (dx = h_w / 2) with their own
+ * N2 disk samples each and a share of the N1 branch-1 samples, and each step
+ * ends with F = renorm_det1(I + dt grad u) from central differences of the
+ * auxiliary velocities.  on = 0 returns to the plain method (F kept, unused).
+ * The grid walk reaches cover * h_w with cover >= sigma_max(F) (rounded up to
+ * 1/16, re-planned between steps when F stretches further, at most 2 = the
+ * reach of the reference's 3x3 walk of 2 h_w cells); min_cover (<= 2) forces
+ * a wider reach.  FP32 only (VPMC_ERR_UNSUPPORTED with precision 64). */
+int vpmc_sim_set_deformation(vpmc_sim* sim, int on, float min_cover);
+/* F of every particle (4N floats); set_F rejects det F <= 0 or non-finite F. */
+int vpmc_sim_set_F(vpmc_sim* sim, const float* F, int is_host);
+int vpmc_sim_get_F(vpmc_sim* sim, float* F, int is_host);
+/* Deformation mode: the five velocities (C, L, R, T, B; u(+) - u(-)) of the
+ * last pass, 10N floats (the reference's velC..velB). */
+int vpmc_sim_get_aux_velocities(vpmc_sim* sim, float* vel5, int is_host);
+/* info[0] = sigma_max of the current F, info[1] = cover in use, info[2] =
+ * particle-steps whose new F stretched beyond 2 (not covered), info[3] = 1 in
+ * deformation mode. */
+int vpmc_sim_deform_info(vpmc_sim* sim, double* info);
+
+/* Reinitialisation (README.md:319-321 and :416-420 of the reference; not in
+ * its code): for every instance, the current field (signed, deformed kernels
+ * in deformation mode) is evaluated at a fresh cell-centred Nx x Ny lattice,
+ * positions move to that lattice, F is reset to the identity, and the
+ * strengths are re-fitted by CG-RBF to the evaluated field (tol, max_iter as
+ * in vpmc_cg_rbf; info: 3 per instance).  Needs N_i = Nx * Ny per instance.
+ * Returns VPMC_ERR_NOT_CONVERGED (after finishing) if some CG did not reach tol. */
+int vpmc_sim_reinit(vpmc_sim* sim, double tol, int max_iter, double* info);
+
+/* Field rasterisation for validation images (the grid diagnostic of
+ * Simulation::test_vorticity_grid, src/vortex_particle_mc.cu:332-456): the
+ * field of instance inst at the cell centres of a res_x x res_y grid over its
+ * domain (ix-major), sign 0 = signed field, +1 / -1 = |omega| of the
+ * positive / negative particles (deformed kernels in deformation mode).
+ * out: res_x * res_y floats (device). */
+int vpmc_sim_vorticity_grid(vpmc_sim* sim, int inst, int res_x, int res_y, int sign, float* out);
 
 /* Change the estimator law / seed / step counter of an existing simulation. */
 int vpmc_sim_set_law(vpmc_sim* sim, int law);

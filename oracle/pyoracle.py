@@ -24,7 +24,8 @@ __all__ = [
     "fill_cells", "counting_sort", "hash_build", "build_subsets", "build_subsets_f64",
     "rcdf", "icdf", "spline_pdf", "spline_mass", "OracleState", "eval_vorticity_cpu",
     "query_vorticity_f64", "field_exact_f64", "mc_estimates", "mc_velocity", "mc_velocity_omp",
-    "rbf_matvec_f64", "cg_rbf_f64", "direct_mollified_f64", "direct_plummer_f64",
+    "rbf_matvec_f64", "cg_rbf_f64", "direct_mollified_f64", "direct_plummer_f64", "direct_deformed_f64",
+    "mc_velocity5_omp",
     "ref_available", "ref_fill_cells", "ref_counting_sort", "ref_build_subsets",
     "ref_rcdf", "ref_icdf", "ref_eval_vorticity", "ref_mc_estimates", "gaussian_field",
 ]
@@ -108,6 +109,8 @@ def lib():
             "orc_rbf_matvec_f64": (None, [vp, vp, vp, db, ip, ip]),
             "orc_cg_rbf_f64": (ip, [vp, vp, vp, db, ip, db, ip, vp, vp, ip]),
             "orc_direct_mollified_f64": (None, [vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
+            "orc_direct_deformed_f64": (None, [vp, vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
+            "orc_mc_velocity5_omp": (ip, [vp, vp, vp, vp, ip, ip, ip, fl, C.c_uint32, vp, ip, vp, ip]),
             "orc_direct_plummer_f64": (None, [vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
             "orc_version": (C.c_char_p, []),
             "orc_rng_create": (vp, [C.c_uint32]),
@@ -403,6 +406,19 @@ def mc_velocity_omp(state: OracleState, targets, N1, N2, seed, nthreads=0, law=0
     return vel, nt
 
 
+def mc_velocity5_omp(state: OracleState, targets, N1, N2, seed, nthreads=0):
+    """The reference GPU kernel's law with deformation (state.F, aux = 1):
+    returns (M, 5, 2) velocities at C, L, R, T, B."""
+    t = np.ascontiguousarray(targets, np.float32)
+    vel = np.zeros((len(t), 5, 2), np.float32)
+    ctx = state.mcctx()
+    tab = icdf(rcdf(state.prm.h_w, 20), state.prm.h_w)
+    nt = lib().orc_mc_velocity5_omp(C.byref(ctx), _ptr(state.pos), _ptr(state.F), _ptr(t), len(t), N1, N2,
+                                    float(np.float32(0.5) * np.float32(state.prm.h_w)), seed, _ptr(vel), nthreads,
+                                    _ptr(tab), len(tab))
+    return vel, nt
+
+
 def rbf_matvec_f64(state: OracleState, x, nthreads=0):
     x = np.ascontiguousarray(x, np.float64)
     y = np.zeros(state.N, np.float64)
@@ -428,6 +444,18 @@ def direct_mollified_f64(pos, omega, pts, h_w, Lx=1.0, Ly=1.0, periodic=True, nt
     out = np.zeros((len(pts), 2), np.float64)
     lib().orc_direct_mollified_f64(_ptr(pos), _ptr(om), len(pos), _ptr(pts), len(pts), h_w, Lx, Ly,
                                    int(periodic), _ptr(out), nthreads)
+    return out
+
+
+def direct_deformed_f64(pos, omega, F, pts, h_w, Lx=1.0, Ly=1.0, periodic=True, nthreads=0):
+    """Velocity of the deformed smoothed field (quadrature, FP64); F (N, 4) or None."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    om = np.ascontiguousarray(omega, np.float32)
+    Fa = None if F is None else np.ascontiguousarray(F, np.float32)
+    pts = np.ascontiguousarray(pts, np.float32)
+    out = np.zeros((len(pts), 2), np.float64)
+    lib().orc_direct_deformed_f64(_ptr(pos), _ptr(om), _ptr(Fa), len(pos), _ptr(pts), len(pts), h_w, Lx, Ly,
+                                  int(periodic), _ptr(out), nthreads)
     return out
 
 

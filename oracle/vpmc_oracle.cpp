@@ -264,7 +264,7 @@ inline f2 mis_term_gpu(f2 dst, f2 sp, float om, float w1, float w2, float cum, f
 // (queryVorticityAbs, here in FP64) and minimum-image alpha/r.
 void mc_estimate(const orc_mcctx& C, const float* pos, const f2* dst, int sign,
                  int aux, int N1, int N2, Rng& g, f2* out, int law = 0,
-                 const float* icdf = nullptr, int icdf_L = 0) {
+                 const float* icdf = nullptr, int icdf_L = 0, const float* Fj = nullptr) {
     const float w1 = float(N1) / float(N1 + N2);
     const float w2 = float(N2) / float(N1 + N2);
     f2 s[5] = {};
@@ -294,8 +294,15 @@ void mc_estimate(const orc_mcctx& C, const float* pos, const f2* dst, int sign,
             const float t = f - i0;
             const float rr = (icdf[i0] * (1.f - t) + icdf[i1] * t) * C.h_w;
             const float th = 2.f * kPiF * unif(g);
-            sp.x += rr * std::cos(th);
-            sp.y += rr * std::sin(th);
+            const float jx = rr * std::cos(th), jy = rr * std::sin(th);
+            if (Fj) {   // mul_mat2(F, r), include/monte_carlo_bs.cuh:99-103
+                const float* f = Fj + 4 * p;
+                sp.x += f[0] * jx + f[1] * jy;
+                sp.y += f[2] * jx + f[3] * jy;
+            } else {
+                sp.x += jx;
+                sp.y += jy;
+            }
             const float om = float(query_vort_f64(V, sp.x, sp.y, sign, false, false, C.h_w, per));
             add(s[0], mis_term_gpu(dst[0], sp, om, w1, w2, cum, alpha_of(dst[0]), per, C.Lx, C.Ly));
             if (aux)
@@ -530,6 +537,28 @@ int orc_mc_velocity_omp(const orc_mcctx* ctx, const float* pos, const float* tar
     return nt;
 }
 
+int orc_mc_velocity5_omp(const orc_mcctx* ctx, const float* pos, const float* F,
+                         const float* targets, int M, int N1, int N2, float dx,
+                         uint32_t seed, float* vel10, int nthreads, const float* icdf,
+                         int icdf_L) {
+    const int nt = threads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
+    for (int t = 0; t < M; ++t) {
+        Rng g(seed + static_cast<uint32_t>(t));
+        const f2 x = ld2(targets, t);
+        // monte_carlo_bs_kernel_safe's auxiliary points (src/cuda/monte_carlo_bs.cu:163-167)
+        const f2 dst[5] = {x, f2{x.x - dx, x.y}, f2{x.x + dx, x.y}, f2{x.x, x.y + dx}, f2{x.x, x.y - dx}};
+        f2 vp[5], vn[5];
+        mc_estimate(*ctx, pos, dst, +1, 1, N1, N2, g, vp, 1, icdf, icdf_L, F);
+        mc_estimate(*ctx, pos, dst, -1, 1, N1, N2, g, vn, 1, icdf, icdf_L, F);
+        for (int a = 0; a < 5; ++a) {
+            vel10[10 * t + 2 * a] = vp[a].x - vn[a].x;
+            vel10[10 * t + 2 * a + 1] = vp[a].y - vn[a].y;
+        }
+    }
+    return nt;
+}
+
 void orc_rbf_matvec_f64(const orc_view* all_view, const double* x, double* y,
                         double h_w, int periodic, int nthreads) {
     const orc_view& V = *all_view;
@@ -642,6 +671,156 @@ void orc_direct_mollified_f64(const float* pos, const float* omega, int N,
                     const double k = spline_mass_d(std::sqrt(r2) / h_w) / (2.0 * kPiD * r2);
                     u += wi * (-dy * k);
                     v += wi * (dx * k);
+                }
+        }
+        out_uv[2 * m] = u;
+        out_uv[2 * m + 1] = v;
+    }
+}
+
+namespace {
+
+// Gauss-Legendre nodes/weights on [-1, 1]: Newton iteration on P_n from the
+// Chebyshev-like initial guesses (the textbook method).
+struct GL {
+    std::vector<double> x, w;
+    explicit GL(int n) : x(n), w(n) {
+        for (int i = 0; i < n; ++i) {
+            double z = std::cos(kPiD * (i + 0.75) / (n + 0.5)), pp = 1.0;
+            for (int it = 0; it < 100; ++it) {
+                double p1 = 1.0, p2 = 0.0;
+                for (int j = 1; j <= n; ++j) {
+                    const double p3 = p2;
+                    p2 = p1;
+                    p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+                }
+                pp = n * (z * p1 - p2) / (z * z - 1.0);
+                const double dz = p1 / pp;
+                z -= dz;
+                if (std::fabs(dz) < 1e-16) break;
+            }
+            x[i] = z;
+            w[i] = 2.0 / ((1.0 - z * z) * pp * pp);
+        }
+    }
+};
+
+// Unnormalised radial profile of the cubic B-spline (utilities.hpp:7-17
+// without the 40/(7 pi h^2) factor) at q = |v|/h.
+inline double spline_shape(double q) {
+    if (q < 0.5) return 6.0 * (q * q * q - q * q) + 1.0;
+    if (q < 1.0) { const double t = 1.0 - q; return 2.0 * t * t * t; }
+    return 0.0;
+}
+
+// g(theta) = integral over rho >= 0 of W-shape(|v + rho e| / h): pieces split
+// where the ray crosses |.| = h/2, h and at its closest approach, GL on each.
+double ray_integral(double vx, double vy, double ex, double ey, double h, const GL& gl) {
+    const double b = vx * ex + vy * ey, c0 = vx * vx + vy * vy;
+    const double dh = b * b - c0 + h * h;
+    if (dh <= 0.0) return 0.0;
+    const double sh = std::sqrt(dh);
+    const double lo = std::max(0.0, -b - sh), hi = -b + sh;
+    if (hi <= lo) return 0.0;
+    double cut[6];
+    int nc = 0;
+    cut[nc++] = lo;
+    const double di = b * b - c0 + 0.25 * h * h;
+    double pts[3];
+    int np = 0;
+    if (di > 0.0) { const double si = std::sqrt(di); pts[np++] = -b - si; pts[np++] = -b + si; }
+    pts[np++] = -b;
+    std::sort(pts, pts + np);
+    for (int k = 0; k < np; ++k) if (pts[k] > lo && pts[k] < hi) cut[nc++] = pts[k];
+    cut[nc++] = hi;
+    double acc = 0.0;
+    for (int k = 0; k + 1 < nc; ++k) {
+        const double a0 = cut[k], a1 = cut[k + 1], hm = 0.5 * (a1 - a0), cm = 0.5 * (a1 + a0);
+        double part = 0.0;
+        for (size_t g = 0; g < gl.x.size(); ++g) {
+            const double r = cm + hm * gl.x[g];
+            const double qx = vx + r * ex, qy = vy + r * ey;
+            part += gl.w[g] * spline_shape(std::sqrt(qx * qx + qy * qy) / h);
+        }
+        acc += hm * part;
+    }
+    return acc;
+}
+
+}  // namespace
+
+void orc_direct_deformed_f64(const float* pos, const float* omega, const float* F, int N,
+                             const float* pts, int M, double h_w, double Lx, double Ly,
+                             int periodic, double* out_uv, int nthreads) {
+    const int nt = threads_or_default(nthreads);
+    const int lo = periodic ? -1 : 0, hi = periodic ? 1 : 0;
+    const double norm = 40.0 / (7.0 * kPiD * h_w * h_w);
+    const GL gr(12), gt(48), gf(10);
+    const int n_trap = 1024;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int m = 0; m < M; ++m) {
+        const double px = pts[2 * m], py = pts[2 * m + 1];
+        double u = 0.0, v = 0.0;
+        for (int i = 0; i < N; ++i) {
+            const double wi = omega[i];
+            if (wi == 0.0) continue;
+            double a = 1, b = 0, c = 0, d = 1;
+            if (F) { a = F[4 * i]; b = F[4 * i + 1]; c = F[4 * i + 2]; d = F[4 * i + 3]; }
+            const double det = a * d - b * c, adet = std::fabs(det);
+            // sigma_max(F): reach of the deformed support
+            const double T = a * a + b * b + c * c + d * d;
+            const double smax = std::sqrt(0.5 * (T + std::sqrt(std::max(T * T - 4.0 * det * det, 0.0))));
+            for (int ix = lo; ix <= hi; ++ix)
+                for (int iy = lo; iy <= hi; ++iy) {
+                    const double rx = px - (double(pos[2 * i]) + ix * Lx);
+                    const double ry = py - (double(pos[2 * i + 1]) + iy * Ly);
+                    const double dist = std::sqrt(rx * rx + ry * ry);
+                    double su = 0.0, sv = 0.0;
+                    if (dist > 3.0 * smax * h_w) {
+                        // smooth kernel over the blob: polar GL in v-space, y = c + F v
+                        for (int pc = 0; pc < 2; ++pc) {
+                            const double r0 = pc == 0 ? 0.0 : 0.5 * h_w, r1 = pc == 0 ? 0.5 * h_w : h_w;
+                            for (size_t g = 0; g < gf.x.size(); ++g) {
+                                const double rr = 0.5 * (r0 + r1) + 0.5 * (r1 - r0) * gf.x[g];
+                                const double wr = 0.5 * (r1 - r0) * gf.w[g] * rr * spline_shape(rr / h_w);
+                                for (int k = 0; k < 64; ++k) {
+                                    const double th = 2.0 * kPiD * (k + 0.5) / 64.0;
+                                    const double vx = rr * std::cos(th), vy = rr * std::sin(th);
+                                    const double dx = rx - (a * vx + b * vy), dy = ry - (c * vx + d * vy);
+                                    const double kk = wr * (2.0 * kPiD / 64.0) / (2.0 * kPiD * (dx * dx + dy * dy));
+                                    su += -dy * kk;
+                                    sv += dx * kk;
+                                }
+                            }
+                        }
+                    } else {
+                        // rays from the singular point v* = F^-1 (x - c): K dv = -perp(F e)/(2 pi |F e|^2) drho dtheta
+                        const double vx = (d * rx - b * ry) / det, vy = (-c * rx + a * ry) / det;
+                        const double vr = std::sqrt(vx * vx + vy * vy);
+                        auto add_dir = [&](double th, double wt) {
+                            const double ex = std::cos(th), ey = std::sin(th);
+                            const double g = ray_integral(vx, vy, ex, ey, h_w, gr);
+                            if (g == 0.0) return;
+                            const double fx = a * ex + b * ey, fy = c * ex + d * ey;
+                            const double s = -wt * g / (2.0 * kPiD * (fx * fx + fy * fy));
+                            su += s * (-fy);
+                            sv += s * fx;
+                        };
+                        if (vr < h_w) {
+                            for (int k = 0; k < n_trap; ++k) add_dir(2.0 * kPiD * k / n_trap, 2.0 * kPiD / n_trap);
+                        } else {
+                            const double phi0 = std::atan2(-vy, -vx), be = std::asin(std::min(1.0, h_w / vr));
+                            const double bi = std::asin(std::min(1.0, 0.5 * h_w / vr));
+                            const double edges[4] = {-be, -bi, bi, be};
+                            for (int pc = 0; pc < 3; ++pc) {
+                                const double t0 = edges[pc], t1 = edges[pc + 1];
+                                for (size_t g = 0; g < gt.x.size(); ++g)
+                                    add_dir(phi0 + 0.5 * (t0 + t1) + 0.5 * (t1 - t0) * gt.x[g], 0.5 * (t1 - t0) * gt.w[g]);
+                            }
+                        }
+                    }
+                    u += wi * adet * norm * su;
+                    v += wi * adet * norm * sv;
                 }
         }
         out_uv[2 * m] = u;

@@ -125,6 +125,15 @@ int  orc_mc_velocity_omp(const orc_mcctx* ctx, const float* pos,
                          uint32_t seed, float* vel, int nthreads,
                          int law, const float* icdf, int icdf_L);
 
+/* The GPU kernel's law (law 1 above) with deformation, as the reference's
+ * step_cuda runs it (aux = 1): views carry F (kernels W(|F^-1 d|)), branch-1
+ * jitter is F r, five targets per particle (C, L, R, T, B at offsets dx).
+ * vel10 = the five u(+) - u(-) per target.  Target t seeded with seed + t. */
+int  orc_mc_velocity5_omp(const orc_mcctx* ctx, const float* pos, const float* F,
+                          const float* targets, int M, int N1, int N2, float dx,
+                          uint32_t seed, float* vel10, int nthreads, const float* icdf,
+                          int icdf_L);
+
 /* ---- RBF system: src/cuda/cg_rbf_init.cu:11-116 restated in FP64 ---- */
 /* y = A x,  A_ij = W(|F_j^-1 (x_j - x_i)|) via the all-particle 3x3 walk. */
 void orc_rbf_matvec_f64(const orc_view* all_view, const double* x, double* y,
@@ -145,6 +154,15 @@ void orc_direct_mollified_f64(const float* pos, const float* omega, int N,
                               const float* pts, int M, double h_w,
                               double Lx, double Ly, int periodic,
                               double* out_uv, int nthreads);
+/* The same velocity for deformed kernels W(|F_i^-1 (y - x_i)|) (F row-major
+ * per particle, NULL = identity): the Biot-Savart integral of each blob by
+ * quadrature in FP64 -- Gauss-Legendre in blob coordinates when the target
+ * is more than 3 sigma_max h_w away, else rays from the target's preimage
+ * (exact ray/circle splits, GL along each ray, trapezoid or windowed GL in
+ * angle).  The mean of the unbiased deformed MIS estimator. */
+void orc_direct_deformed_f64(const float* pos, const float* omega, const float* F, int N,
+                             const float* pts, int M, double h_w, double Lx, double Ly,
+                             int periodic, double* out_uv, int nthreads);
 /* biot_savart_naive_kernel (src/cuda/naive_biot_savart.cu:15-40) in FP64:
  * Plummer core eps, minimum image, j == i skipped.  Targets are particle
  * indices. */

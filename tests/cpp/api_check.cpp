@@ -90,14 +90,19 @@ int main(int argc, char** argv) {
         std::vector<double> gerr{grid_err};
         dump("grid_err", gerr);
 
-        sim.step_cuda(true);
+        sim.step_cuda(true);   // the reference's step: deformed kernels, aux points, F update
         dump("pos1", sim.particles_.pos.to_host());
         dump("vel1", sim.particles_.vel.to_host());
+        dump("F1", sim.particles_.F.to_host());
 
         std::vector<float2> before = sim.particles_.pos.to_host();
         sim.step_cuda_naive(true);
         dump("pos_naive_before", before);
         dump("pos_naive_after", sim.particles_.pos.to_host());
+
+        const std::vector<double> rinfo = sim.reinitialize(1e-8, 1000);
+        dump("pos_reinit", sim.particles_.pos.to_host());
+        dump("reinit_info", rinfo);
 
         const float2 d{0.3f, 0.7f};
         flags[4] = SamplingDiskRadius(d, true, 1.f, 1.f) > 1.41f && SamplingDiskRadius(d, true, 1.f, 1.f) < 1.42f;

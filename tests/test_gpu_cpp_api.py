@@ -69,6 +69,10 @@ def test_matvec_step_and_naive_step(run):
     assert run("grid_err", np.float64)[0] < 1e-4 * np.abs(omega).max() * 100
     p1, v1 = run("pos1", np.float32).reshape(-1, 2), run("vel1", np.float32).reshape(-1, 2)
     assert np.isfinite(v1).all() and np.abs(v1).max() > 0
+    # step_cuda updated F (update_jacobian_from5 + renorm_det1): det 1, not the identity
+    F1 = run("F1", np.float32).reshape(-1, 4)[: len(p1)]
+    det = F1[:, 0] * F1[:, 3] - F1[:, 1] * F1[:, 2]
+    assert np.abs(det - 1).max() < 1e-5 and np.abs(F1 - [1, 0, 0, 1]).max() > 1e-4
     w = pos.astype(np.float64) + np.float64(np.float32(1e-3)) * v1.astype(np.float64)
     w = (w - np.floor(w)).astype(np.float32)
     w[w >= 1] = 0
@@ -79,4 +83,8 @@ def test_matvec_step_and_naive_step(run):
     w = (w - np.floor(w))
     d = np.abs(pa - w)
     d = np.minimum(d, 1 - d)
-    assert d.max() < 1e-6
+    # reinitialize: back on the lattice, CG converged
+    assert np.array_equal(run("pos_reinit", np.float32).reshape(-1, 2), O.lattice(64))
+    assert run("reinit_info", np.float64)[2] < 1e-5
+    # FP32 velocities (the reference's naive kernel is FP32): 1e-4 relative on u, times dt
+    assert d.max() < 1e-6 + 1e-3 * 1e-4 * np.abs(u).max()

@@ -1,0 +1,62 @@
+"""Reinitialisation (remesh to the lattice, F = I, CG refit) and the field
+raster used for validation images, on the GPU, against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(cuda, Nx=64, hwr=4, law=1, deform=True):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    pos = O.lattice(Nx)
+    prm = O.SimParam(dt=2e-3, Nx=Nx, hwr=hwr, N1=16, N2=16)
+    om = (O.taylor_green(pos) * np.float32(prm.h * prm.h)).astype(np.float32)
+    sim = P.Simulation(P.SimParam(dt=2e-3, Nx=Nx, hwr=hwr, N1=16, N2=16, law=law, seed=5), [len(pos)])
+    sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+    sim.prepare()
+    if deform:
+        sim.set_deformation(True)
+    return sim, pos, prm
+
+
+@pytest.mark.parametrize("deform", [True, False])
+def test_reinit_remeshes_resets_F_and_refits_the_field(cuda, deform):
+    sim, lat, prm = _sim(cuda, deform=deform)
+    sim.step(3)
+    p0, om0, _ = (t.cpu().numpy() for t in sim.particles())
+    F0 = sim.F().cpu().numpy()
+    assert not np.array_equal(p0, lat)
+    info = sim.reinit(tol=1e-9, max_iter=2000)[0]
+    p1, om1, _ = (t.cpu().numpy() for t in sim.particles())
+    assert np.array_equal(p1, lat)
+    assert np.array_equal(sim.F().cpu().numpy(), np.tile(np.array([1, 0, 0, 1], np.float32), (len(lat), 1)))
+    # the field the refit must reproduce: old particles (and F) evaluated at the lattice
+    st0 = O.OracleState(p0, om0, prm, F=F0 if deform else None)
+    b = O.query_vorticity_f64(st0.view("all"), lat, 0, True, False, prm.h_w, True)
+    st1 = O.OracleState(lat, om1, prm)
+    Aw = O.rbf_matvec_f64(st1, om1.astype(np.float64))
+    assert np.linalg.norm(Aw - b) <= 1e-5 * np.linalg.norm(b), (info, np.linalg.norm(Aw - b) / np.linalg.norm(b))
+    # stepping continues from the reinitialised state
+    sim.step(1)
+    assert np.isfinite(sim.particles()[0].cpu().numpy()).all()
+
+
+def test_vorticity_grid_matches_oracle_and_writes_pgm(cuda, tmp_path):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    sim, lat, prm = _sim(cuda, deform=True)
+    sim.step(2)
+    p0, om0, _ = (t.cpu().numpy() for t in sim.particles())
+    st = O.OracleState(p0, om0, prm, F=sim.F().cpu().numpy())
+    gx, gy = 48, 40
+    pts = O.lattice(gx, gy)
+    for sign, which in [(0, "all"), (1, "pos"), (-1, "neg")]:
+        got = sim.vorticity_grid(gx, gy, sign=sign).cpu().numpy()
+        want = O.query_vorticity_f64(st.view(which), pts, sign, sign == 0, False, prm.h_w, True).reshape(gx, gy)
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max(), sign
+    path = tmp_path / "vort.pgm"
+    P.write_pgm(str(path), sim.vorticity_grid(gx, gy))
+    data = path.read_bytes()
+    assert data.startswith(b"P5\n48 40\n255\n") and len(data) == len(b"P5\n48 40\n255\n") + gx * gy

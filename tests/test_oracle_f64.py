@@ -95,3 +95,32 @@ def test_plummer_matches_bruteforce():
         c = 1.0 / (2 * np.pi * ((d ** 2).sum(1) + 0.05 ** 2))
         c[i] = 0
         np.testing.assert_allclose(u[m], [(om * -d[:, 1] * c).sum(), (om * d[:, 0] * c).sum()], rtol=1e-10, atol=1e-12)
+
+
+def test_deformed_quadrature_reduces_to_mollified_and_is_rotation_invariant():
+    """F = I: the quadrature equals the closed-form mollified sum; F a rotation:
+    the same field (W is radial); sheared F: continuous across the switch
+    between its two quadratures, point-vortex-like far away."""
+    rng = np.random.default_rng(3)
+    pos = rng.random((300, 2)).astype(np.float32)
+    om = rng.normal(size=300).astype(np.float32)
+    pts = rng.random((16, 2)).astype(np.float32)
+    h = 0.0625
+    a = O.direct_mollified_f64(pos, om, pts, h)
+    b = O.direct_deformed_f64(pos, om, None, pts, h)
+    assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max()
+    th = rng.random(300) * 2 * np.pi
+    R = np.stack([np.cos(th), -np.sin(th), np.sin(th), np.cos(th)], 1).astype(np.float32)
+    c = O.direct_deformed_f64(pos, om, R, pts, h)
+    assert np.abs(a - c).max() <= 1e-7 * np.abs(a).max()
+    s = 0.6
+    Fs = np.array([[1, s, 0, 1]], np.float32)
+    T = 2 + s * s
+    smax = np.sqrt(0.5 * (T + np.sqrt(T * T - 4)))
+    one = np.array([[0.5, 0.5]], np.float32)
+    u = [O.direct_deformed_f64(one, np.ones(1, np.float32), Fs, np.array([[0.5 + d, 0.5]], np.float32), h,
+                               periodic=False)[0] for d in (3 * smax * h * (1 - 1e-7), 3 * smax * h * (1 + 1e-7))]
+    assert np.abs(u[0] - u[1]).max() <= 1e-6 * np.abs(u[0]).max()
+    far = O.direct_deformed_f64(one, np.ones(1, np.float32), Fs, np.array([[0.5 + 40 * h, 0.5]], np.float32), h,
+                                periodic=False)[0]
+    assert abs(far[1] - 1 / (2 * np.pi * 40 * h)) < 1e-3 * far[1]

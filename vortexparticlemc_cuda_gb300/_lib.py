@@ -63,6 +63,7 @@ SIGNATURES = {
     "vpmc_cg_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_cg_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_direct_velocity_f64": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _d, _i, _vp]),
+    "vpmc_direct_velocity_f32": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _f, _f, _f, _i, _vp]),
     "vpmc_sim_create": (_i, [_vp, _i, _vp, _vp, C.POINTER(_vp)]),
     "vpmc_sim_destroy": (_i, [_vp]),
     "vpmc_sim_num_particles": (_i, [_vp]),
@@ -75,6 +76,13 @@ SIGNATURES = {
     "vpmc_sim_step_host": (_i, [_vp, _vp, _vp, _vp]),
     "vpmc_advect": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i]),
     "vpmc_sim_set_law": (_i, [_vp, _i]),
+    "vpmc_sim_set_deformation": (_i, [_vp, _i, _f]),
+    "vpmc_sim_reinit": (_i, [_vp, _d, _i, _vp]),
+    "vpmc_sim_vorticity_grid": (_i, [_vp, _i, _i, _i, _i, _vp]),
+    "vpmc_sim_set_F": (_i, [_vp, _vp, _i]),
+    "vpmc_sim_get_F": (_i, [_vp, _vp, _i]),
+    "vpmc_sim_get_aux_velocities": (_i, [_vp, _vp, _i]),
+    "vpmc_sim_deform_info": (_i, [_vp, _vp]),
     "vpmc_sim_set_seed": (_i, [_vp, _u64]),
     "vpmc_sim_set_step": (_i, [_vp, _u64]),
     "vpmc_sim_get_step": (_u64, [_vp]),

@@ -2,6 +2,7 @@
 // the field-evaluation kernel (the hot loop of queries, MIS samples and SpMV).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "vpmc_grid.cuh"
@@ -82,6 +83,53 @@ __global__ void k_grid_gather(const uint32_t* __restrict__ perm, const uint32_t*
     }
 }
 
+// Deformed records: metric G = F^-T F^-1 of F = [[F.x, F.y], [F.z, F.w]]
+// (the inverse the reference applies, include/vorticity_query.cuh:52-63,
+// divides the adjugate by det F), formed in FP64.
+__global__ void k_grid_gather_f(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ start, long n,
+                                uint32_t nbins, const float2* __restrict__ pos, const float* __restrict__ omega,
+                                const float4* __restrict__ F, const GridInst* __restrict__ inst, int n_inst,
+                                int set_mode, CandF* __restrict__ cand) {
+    const long nv = start[nbins];
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x) {
+        const uint32_t i = perm[p];
+        const GridInst G = inst[inst_of_particle(inst, n_inst, i)];
+        float2 q = pos[i];
+        if (G.periodic) { q.x = wrapf(q.x, G.Lx); q.y = wrapf(q.y, G.Ly); }
+        const float w = omega ? omega[i] : 1.f;
+        const double wd = double(set_mode == SET_ONE_SIGNED ? w : fabsf(w)) * (80.0 / (7.0 * kPiD * double(G.hw) * G.hw));
+        const float wt = float(wd);
+        const float4 f = F[i];
+        const double det = double(f.x) * f.w - double(f.y) * f.z;
+        const double id2 = 1.0 / (det * det);
+        CandF r;
+        r.f[0] = q.x;
+        r.f[1] = q.y;
+        r.f[2] = float((double(f.w) * f.w + double(f.z) * f.z) * id2);
+        r.f[3] = float(-(double(f.w) * f.y + double(f.z) * f.x) * id2);
+        r.f[4] = float((double(f.y) * f.y + double(f.x) * f.x) * id2);
+        r.f[5] = wt;
+        r.f[6] = float(wd - double(wt));
+#pragma unroll
+        for (int k = 7; k < 16; ++k) r.f[k] = 0.f;
+        cand[p] = r;
+    }
+}
+
+__global__ void k_sigma(const float4* __restrict__ F, long n, unsigned* __restrict__ out) {
+    unsigned m = 0u;
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const float4 f = F[i];
+        const float sm = sigma_max(f);
+        const float det = f.x * f.w - f.y * f.z;
+        // non-negative floats order as their bit patterns; degenerate F -> +inf
+        m = max(m, (sm == sm && sm <= 3.0e38f && det > 0.f) ? __float_as_uint(sm) : 0x7f800000u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 __global__ void k_grid_weights(const double* __restrict__ x, long n, double scale, Cand* __restrict__ cand) {
     for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += long(gridDim.x) * blockDim.x) {
         const double v = x[p] * scale;
@@ -159,6 +207,80 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
     }
 }
 
+// Two-pass placement of ranked samples.  The final slot of sample m is
+// qstart[bin] + qrank[m]; writing 16-byte records straight there touches a
+// different DRAM sector per sample (the bins of consecutive samples are
+// unrelated), so the placement goes through coarse super-bins (2^S
+// consecutive bins): pass 1 moves each CTA's tile of samples into runs per
+// super-bin (one global atomic per CTA and super-bin), pass 2 streams the
+// super-bin segments and writes each record to its final slot -- a region
+// the size of one super-bin at a time, which stays in L2 until it is full.
+constexpr int kCoarseTile = 16;   // samples per thread per tile
+constexpr int kMaxSuper = 2048;
+
+__global__ void __launch_bounds__(256) k_scatter_coarse(const float2* __restrict__ pts, long M,
+                                                         const GridInst* __restrict__ inst, int n_inst,
+                                                         const uint32_t* __restrict__ qbin,
+                                                         const uint32_t* __restrict__ qrank,
+                                                         const uint32_t* __restrict__ qstart, int shift, int nsuper,
+                                                         uint32_t* __restrict__ super_fill, uint4* __restrict__ tmp) {
+    __shared__ uint32_t hist[kMaxSuper];
+    const long tile = long(kCoarseTile) * blockDim.x;
+    for (long t0 = long(blockIdx.x) * tile; t0 < M; t0 += long(gridDim.x) * tile) {
+        for (int k = threadIdx.x; k < nsuper; k += blockDim.x) hist[k] = 0u;
+        __syncthreads();
+        uint32_t sb[kCoarseTile], lr[kCoarseTile];
+#pragma unroll
+        for (int j = 0; j < kCoarseTile; ++j) {
+            const long m = t0 + long(j) * blockDim.x + threadIdx.x;
+            sb[j] = kNoBin;
+            if (m < M) {
+                const uint32_t b = qbin[m];
+                if (b != kNoBin) {
+                    sb[j] = b >> shift;
+                    lr[j] = atomicAdd(&hist[sb[j]], 1u);
+                }
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < nsuper; k += blockDim.x) {
+            const uint32_t c = hist[k];
+            if (c) hist[k] = qstart[uint32_t(k) << shift] + atomicAdd(&super_fill[k], c);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kCoarseTile; ++j) {
+            if (sb[j] == kNoBin) continue;
+            const long m = t0 + long(j) * blockDim.x + threadIdx.x;
+            const uint32_t b = qbin[m];
+            const GridInst& G = inst[inst_of_bin(inst, n_inst, b)];
+            float2 p = pts[m];
+            uint32_t ikx = 2u, iky = 2u;
+            if (G.periodic) {
+                const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+                p.x = p.x - kx * G.Lx;
+                p.y = p.y - ky * G.Ly;
+                ikx = uint32_t(min(max(int(kx), -2), 2) + 2);
+                iky = uint32_t(min(max(int(ky), -2), 2) + 2);
+            }
+            const uint32_t slot = qstart[b] + qrank[m];
+            tmp[hist[sb[j]] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y),
+                                                  uint32_t(m) | (ikx << 29), slot | (iky << 29));
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_scatter_fine(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total, long M,
+                               QRec* __restrict__ qrec) {
+    const long n = min(long(*total), M);
+    constexpr uint32_t low = (1u << 29) - 1u;
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const uint4 r = tmp[i];
+        qrec[r.w & low] = QRec{__uint_as_float(r.x), __uint_as_float(r.y), r.z & low, (r.z >> 29) | ((r.w >> 29) << 3)};
+    }
+}
+
 __global__ void k_items_count(const uint32_t* __restrict__ qstart, long nbins, int chunk,
                               uint32_t* __restrict__ per_bin) {
     for (long b = long(blockIdx.x) * blockDim.x + threadIdx.x; b < nbins; b += long(gridDim.x) * blockDim.x) {
@@ -200,6 +322,7 @@ struct EvalArgs {
     const GridInst* inst;
     const uint32_t* cstart;
     const Cand* cand;
+    const CandF* candf;
     const QRec* qrec;
     const Item* items;
     const uint32_t* n_items;
@@ -283,6 +406,43 @@ __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt,
     }
 }
 
+// The same sum for deformed kernels: r^2 from the expanded metric form
+// (5 packed FMAs instead of 3), the spline as above.
+template <int NPR, int NPMAX>
+__device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int cnt, const f2x (&QXX)[NPMAX],
+                                             const f2x (&QXY)[NPMAX], const f2x (&QYY)[NPMAX],
+                                             const f2x (&QX)[NPMAX], const f2x (&QY)[NPMAX], f2x (&P)[NPMAX],
+                                             float A, float B, float ih) {
+    const f2x HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
+    const f2x A2 = pk2(A, A), B2 = pk2(B, B), NIH = pk2(-ih, -ih);
+#pragma unroll 2
+    for (int c = 0; c < cnt; ++c) {
+        const ulonglong2* rec = reinterpret_cast<const ulonglong2*>(cs[c].f);
+        const ulonglong2 R0 = rec[0];   // (g11), (2 g12)
+        const ulonglong2 R1 = rec[1];   // (g22), (a)
+        const ulonglong2 R2 = rec[2];   // (b), (e)
+        const ulonglong2 R3 = rec[3];   // (w), (0)
+#pragma unroll
+        for (int pr = 0; pr < NPR; ++pr) {
+            f2x r2p = fma2(R0.x, QXX[pr], R2.y);
+            r2p = fma2(R0.y, QXY[pr], r2p);
+            r2p = fma2(R1.x, QYY[pr], r2p);
+            r2p = fma2(R1.y, QX[pr], r2p);
+            r2p = fma2(R2.x, QY[pr], r2p);
+            float ra, rb;
+            up2(r2p, ra, rb);
+            const f2x r = pk2(sqrt_approx(fabsf(ra)), sqrt_approx(fabsf(rb)));
+            const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
+            const f2x t = fma2(NIH, r, ONE);
+            const f2x t3 = mul2(mul2(t, t), t);
+            float ia, ib, ta, tb;
+            up2(in, ia, ib);
+            up2(t3, ta, tb);
+            P[pr] = fma2(R3.x, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+        }
+    }
+}
+
 template <int MODE, int QPT>
 __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     extern __shared__ __align__(128) Cand s_cand[];
@@ -296,7 +456,13 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
     constexpr bool kField64 = MODE == EVAL_FIELD64 || MODE == EVAL_FIELD9_64;
-    constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9;
+    constexpr bool kDef = eval_deformed(MODE);
+    constexpr bool kDefExc = MODE == EVAL_FIELD_F_EXC;
+    constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9 || MODE == EVAL_FIELD_F || MODE == EVAL_FIELD9_F;
+    constexpr bool kField9 = MODE == EVAL_FIELD9 || MODE == EVAL_FIELD9_64 || MODE == EVAL_FIELD9_F;
+    constexpr uint32_t kRec = kDef ? uint32_t(sizeof(CandF)) : uint32_t(sizeof(Cand));
+    constexpr int kCap = kDef ? kCandCap / 2 : kCandCap;   // records per staged batch
+    CandF* const s_candf = reinterpret_cast<CandF*>(s_cand);
     constexpr int NP = QPT / 2;   // packed query pairs
     static_assert(!kPacked || (QPT % 2 == 0), "packed path needs an even query count");
     using Acc = typename std::conditional<kF64 || kField64, double, float>::type;
@@ -386,9 +552,9 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 int pc = s_cur_piece;
                 uint32_t po = s_cur_off, tot = 0;
                 int nb = 0;
-                while (pc < s_np && tot < uint32_t(kCandCap) && nb < kMaxPieces + 2) {
+                while (pc < s_np && tot < uint32_t(kCap) && nb < kMaxPieces + 2) {
                     const uint32_t rem = s_pc[pc].cnt - po;
-                    const uint32_t take = min(rem, uint32_t(kCandCap) - tot);
+                    const uint32_t take = min(rem, uint32_t(kCap) - tot);
                     s_bp[nb++] = BatchPiece{tot, take, s_pc[pc].gstart + po, pc};
                     tot += take;
                     po += take;
@@ -400,10 +566,12 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 s_btot = tot;
                 if (tot > 0) {
                     fence_proxy_async_smem();
-                    mbar_arrive_expect_tx(&s_bar, tot * uint32_t(sizeof(Cand)));
+                    mbar_arrive_expect_tx(&s_bar, tot * kRec);
+                    const char* gsrc = kDef ? reinterpret_cast<const char*>(a.candf)
+                                            : reinterpret_cast<const char*>(a.cand);
                     for (int b = 0; b < nb; ++b)
-                        bulk_g2s(&s_cand[s_bp[b].soff], &a.cand[s_bp[b].gstart],
-                                 s_bp[b].cnt * uint32_t(sizeof(Cand)), &s_bar);
+                        bulk_g2s(reinterpret_cast<char*>(s_cand) + size_t(s_bp[b].soff) * kRec,
+                                 gsrc + size_t(s_bp[b].gstart) * kRec, s_bp[b].cnt * kRec, &s_bar);
                 }
             }
             __syncthreads();
@@ -421,15 +589,31 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                     const Piece pc = s_pc[bp.piece];
                     const float ox = s_ox + pc.qdx, oy = s_oy + pc.qdy;
                     for (uint32_t c = threadIdx.x; c < bp.cnt; c += kEvalThreads) {
-                        Cand& cd = s_cand[bp.soff + c];
-                        const float lx = cd.x - ox, ly = cd.y - oy;
-                        const float c2 = fmaf(lx, lx, ly * ly);
-                        cd.x = lx;
-                        cd.x2 = lx;
-                        cd.y = ly;
-                        cd.y2 = ly;
-                        cd.wl = c2;
-                        cd.pad = c2;
+                        if constexpr (kDef) {
+                            float* f = s_candf[bp.soff + c].f;
+                            const float lx = f[0] - ox, ly = f[1] - oy;
+                            const float g11 = f[2], g12 = f[3], g22 = f[4], w = f[5];
+                            const float gx = fmaf(g11, lx, g12 * ly), gy = fmaf(g12, lx, g22 * ly);
+                            const float e = fmaf(lx, gx, ly * gy);
+                            f[0] = g11; f[1] = g11;
+                            f[2] = 2.f * g12; f[3] = 2.f * g12;
+                            f[4] = g22; f[5] = g22;
+                            f[6] = -2.f * gx; f[7] = -2.f * gx;
+                            f[8] = -2.f * gy; f[9] = -2.f * gy;
+                            f[10] = e; f[11] = e;
+                            f[12] = w; f[13] = w;
+                            f[14] = 0.f; f[15] = 0.f;
+                        } else {
+                            Cand& cd = s_cand[bp.soff + c];
+                            const float lx = cd.x - ox, ly = cd.y - oy;
+                            const float c2 = fmaf(lx, lx, ly * ly);
+                            cd.x = lx;
+                            cd.x2 = lx;
+                            cd.y = ly;
+                            cd.y2 = ly;
+                            cd.wl = c2;
+                            cd.pad = c2;
+                        }
                     }
                 }
                 __syncthreads();
@@ -440,7 +624,33 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 const Cand* cs = s_cand + bp.soff;
                 const int cnt = int(bp.cnt);
                 Acc part[QPT];
-                if constexpr (kPacked) {
+                if constexpr (kPacked && kDef) {
+                    // queries in the local frame: the monomials of the expanded metric form
+                    f2x QXX[NP], QXY[NP], QYY[NP], QX[NP], QY[NP], P[NP];
+#pragma unroll
+                    for (int pr = 0; pr < NP; ++pr) {
+                        const float ax = qx[2 * pr] - s_ox, bx = qx[2 * pr + 1] - s_ox;
+                        const float ay = qy[2 * pr] - s_oy, by = qy[2 * pr + 1] - s_oy;
+                        QXX[pr] = pk2(ax * ax, bx * bx);
+                        QXY[pr] = pk2(ax * ay, bx * by);
+                        QYY[pr] = pk2(ay * ay, by * by);
+                        QX[pr] = pk2(ax, bx);
+                        QY[pr] = pk2(ay, by);
+                        P[pr] = pk2(0.f, 0.f);
+                    }
+                    const CandF* csf = s_candf + bp.soff;
+                    if (nq <= 2) packed_run_f<1, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
+                    else if (NP >= 2 && nq <= 4)
+                        packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
+                    else packed_run_f<NP, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
+#pragma unroll
+                    for (int pr = 0; pr < NP; ++pr) {
+                        float lo, hi;
+                        up2(P[pr], lo, hi);
+                        part[2 * pr] = lo;
+                        part[2 * pr + 1] = hi;
+                    }
+                } else if constexpr (kPacked) {
                     // queries in the same local frame: -2 q and |q|^2
                     f2x QX[NP], QY[NP], Q2[NP], P[NP];
 #pragma unroll
@@ -462,6 +672,33 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                         up2(P[pr], lo, hi);
                         part[2 * pr] = lo;
                         part[2 * pr + 1] = hi;
+                    }
+                } else if constexpr (kDefExc) {
+                    // deformed kernels, differences taken directly (an exact zero
+                    // for coincident points, so the centre test is reliable)
+                    float px[QPT], py[QPT];
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        px[j] = qx[j] + pc.qdx;
+                        py[j] = qy[j] + pc.qdy;
+                        part[j] = Acc(0);
+                    }
+                    const float A = G.A, B = G.B, ih = G.inv_hw;
+                    const CandF* csf = s_candf + bp.soff;
+                    for (int c = 0; c < cnt; ++c) {
+                        const float cx = csf[c].f[0], cy = csf[c].f[1];
+                        const float g11 = csf[c].f[2], g12 = csf[c].f[3], g22 = csf[c].f[4], cw = csf[c].f[5];
+#pragma unroll
+                        for (int j = 0; j < QPT; ++j) {
+                            const float dx = cx - px[j], dy = cy - py[j];
+                            const float r2 = fmaf(g11 * dx, dx, fmaf(2.f * g12 * dx, dy, g22 * dy * dy));
+                            const float r = sqrtf(fmaxf(r2, 0.f));
+                            const float inner = fmaf(r2, fmaf(A, r, B), 0.5f);
+                            const float t = fmaf(-ih, r, 1.0f);
+                            float v = fmaxf(fminf(inner, t * t * t), 0.0f);
+                            if (r < 1e-6f) v = 0.f;
+                            part[j] = fmaf(cw, v, part[j]);
+                        }
                     }
                 } else if constexpr (kField64) {
                     // the plain FP64 path: every pair and the sum in FP64
@@ -540,7 +777,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 #pragma unroll
                 for (int j = 0; j < QPT; ++j) {
                     bool use = true;
-                    if (MODE == EVAL_FIELD9 || MODE == EVAL_FIELD9_64) {
+                    if (kField9) {
                         const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
                         use = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
                     }
@@ -614,10 +851,12 @@ long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     for (int i = 0; i < n; ++i) {
         const InstDesc& d = in[i];
         if (!(d.hw > 0.f) || !(d.Lx > 0.f) || !(d.Ly > 0.f)) return -VPMC_ERR_INVALID;
+        if (!(d.cover >= 1.f)) return -VPMC_ERR_INVALID;
+        const double reach = double(d.hw) * double(d.cover);   // physical support radius to cover
         int kk = k, gx = 0, gy = 0;
         for (; kk >= 1; --kk) {
-            gx = int(std::floor(double(kk) * double(d.Lx) / double(d.hw) + 1e-9));
-            gy = int(std::floor(double(kk) * double(d.Ly) / double(d.hw) + 1e-9));
+            gx = int(std::floor(double(kk) * double(d.Lx) / reach + 1e-9));
+            gy = int(std::floor(double(kk) * double(d.Ly) / reach + 1e-9));
             if (!d.periodic || (gx >= 2 * kk + 1 && gy >= 2 * kk + 1)) break;
         }
         if (kk < 1 || gx < 1 || gy < 1) return -VPMC_ERR_GEOMETRY;
@@ -648,7 +887,7 @@ long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     return base;
 }
 
-void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g) {
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed) {
     g->inst = c.take<GridInst>(size_t(n_inst));
     g->n_inst = n_inst;
     g->nbins = nbins;
@@ -657,13 +896,16 @@ void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g) {
     g->count = c.take<uint32_t>(size_t(nbins + 1));
     g->start = c.take<uint32_t>(size_t(nbins + 1));
     g->cand = c.take<Cand>(size_t(n < 1 ? 1 : n));
+    g->candf = deformed ? c.take<CandF>(size_t(n < 1 ? 1 : n)) : nullptr;
     carve_radix(c, n, &g->rs);
     // the bin scan reuses the radix scan scratch when it is large enough
     const size_t need = scan_tmp_elems(nbins + 1);
     if (need > scan_tmp_elems(long(radix_counts_elems(n)))) g->rs.scan_tmp = c.take<uint32_t>(need + 1);
 }
 
-int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode) {
+int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode,
+               const float4* F) {
+    if (F && !g.candf) return VPMC_ERR_INVALID;
     cudaStream_t st = ctx->stream;
     VPMC_CUDA(cudaMemsetAsync(g.count, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
     VPMC_LAUNCH(k_grid_keys, blocks_for(g.n), 256, 0, st, pos, omega, g.n, g.inst, g.n_inst, set_mode,
@@ -672,13 +914,31 @@ int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* o
     uint32_t *ks = nullptr, *vs = nullptr;
     VPMC_TRY(radix_sort(ctx, g.keys, nullptr, g.n, bits_for(uint64_t(g.nbins) + 1), g.rs, &ks, &vs));
     g.perm = vs;
-    VPMC_LAUNCH(k_grid_gather, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega,
-                g.inst, g.n_inst, set_mode, g.cand);
+    if (F)
+        VPMC_LAUNCH(k_grid_gather_f, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega, F,
+                    g.inst, g.n_inst, set_mode, g.candf);
+    else
+        VPMC_LAUNCH(k_grid_gather, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega,
+                    g.inst, g.n_inst, set_mode, g.cand);
     return VPMC_OK;
 }
 
 int grid_set_weights_sorted(vpmc_context* ctx, GridBufs& g, const double* x_sorted, double scale) {
     VPMC_LAUNCH(k_grid_weights, blocks_for(g.n), 256, 0, ctx->stream, x_sorted, g.n, scale, g.cand);
+    return VPMC_OK;
+}
+
+int grid_max_sigma(vpmc_context* ctx, const float4* F, long n, unsigned* d_words, float* sigma) {
+    cudaStream_t st = ctx->stream;
+    VPMC_CUDA(cudaMemsetAsync(d_words, 0, 2 * sizeof(unsigned), st));
+    if (n > 0)
+        VPMC_LAUNCH(k_sigma, std::min(blocks_for(n), 4 * ctx->sm_count), 256, 0, st, F, n, d_words);
+    unsigned h = 0u;
+    VPMC_CUDA(cudaMemcpyAsync(&h, d_words, sizeof(h), cudaMemcpyDeviceToHost, st));
+    VPMC_CUDA(cudaStreamSynchronize(st));
+    float v;
+    memcpy(&v, &h, sizeof(v));
+    *sigma = n > 0 ? v : 1.f;
     return VPMC_OK;
 }
 
@@ -701,7 +961,7 @@ int make_items(vpmc_context* ctx, const GridBufs& g, const uint32_t* qstart, Ite
     return VPMC_OK;
 }
 
-void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q) {
+void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool two_pass) {
     const size_t m = size_t(max_points < 1 ? 1 : max_points);
     q->qbin = c.take<uint32_t>(m);
     q->qcount = c.take<uint32_t>(size_t(nbins + 1));
@@ -709,6 +969,8 @@ void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q) {
     q->qfill = c.take<uint32_t>(size_t(nbins + 1));
     q->qrank = c.take<uint32_t>(m);
     q->qrec = c.take<QRec>(m);
+    q->tmp = two_pass ? c.take<uint4>(m) : nullptr;
+    q->super_fill = two_pass ? c.take<uint32_t>(kMaxSuper + 1) : nullptr;
     q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
 }
 
@@ -724,6 +986,19 @@ int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
 
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M) {
     VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
+    if (q.tmp && M <= (1L << 29)) {   // sample ids and slots fit 29 bits
+        int shift = 0;
+        while (((g.nbins - 1) >> shift) + 1 > kMaxSuper / 2) ++shift;
+        const int nsuper = int(((g.nbins - 1) >> shift) + 1);
+        cudaStream_t st = ctx->stream;
+        VPMC_CUDA(cudaMemsetAsync(q.super_fill, 0, sizeof(uint32_t) * size_t(nsuper), st));
+        const long tiles = (M + kCoarseTile * 256 - 1) / (kCoarseTile * 256);
+        const int grid = int(std::min<long>(tiles, 8L * ctx->sm_count));
+        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), 256, 0, st, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,
+                    q.qstart, shift, nsuper, q.super_fill, q.tmp);
+        VPMC_LAUNCH(k_scatter_fine, blocks_for(M), 256, 0, st, q.tmp, q.qstart + g.nbins, M, q.qrec);
+        return VPMC_OK;
+    }
     VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, ctx->stream, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,
                 q.qstart, q.qrec);
     return VPMC_OK;
@@ -737,7 +1012,8 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 }
 
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
-    EvalArgs a{g.inst, g.start, g.cand, qrec, it.items, it.n_items, it.counter, L.out_f32, L.out_f64, ctx->d_flags};
+    if (eval_deformed(L.mode) && !g.candf) return VPMC_ERR_INVALID;
+    EvalArgs a{g.inst, g.start, g.cand, g.candf, qrec, it.items, it.n_items, it.counter, L.out_f32, L.out_f64, ctx->d_flags};
     switch (L.mode) {
         case EVAL_FIELD:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);
@@ -754,6 +1030,15 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
         case EVAL_SPMV32:
             if (L.qpt != 4) return VPMC_ERR_INVALID;
             return launch_eval_t<EVAL_SPMV32, 4>(ctx, a);
+        case EVAL_FIELD_F:
+            if (L.qpt == 8) return launch_eval_t<EVAL_FIELD_F, 8>(ctx, a);
+            return launch_eval_t<EVAL_FIELD_F, 4>(ctx, a);
+        case EVAL_FIELD9_F:
+            if (L.qpt == 8) return launch_eval_t<EVAL_FIELD9_F, 8>(ctx, a);
+            return launch_eval_t<EVAL_FIELD9_F, 4>(ctx, a);
+        case EVAL_FIELD_F_EXC:
+            if (L.qpt != 4) return VPMC_ERR_INVALID;
+            return launch_eval_t<EVAL_FIELD_F_EXC, 4>(ctx, a);
         case EVAL_FIELD64: return launch_eval_t<EVAL_FIELD64, 4>(ctx, a);
         case EVAL_FIELD9_64: return launch_eval_t<EVAL_FIELD9_64, 4>(ctx, a);
         default: return VPMC_ERR_INVALID;

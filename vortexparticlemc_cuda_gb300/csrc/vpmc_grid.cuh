@@ -42,6 +42,17 @@ struct __align__(16) Cand {
     float w, w2, wl, pad;
 };
 
+// Candidate record of a deformed kernel W(|F^-1 d|) (64 bytes).  In global
+// memory: f = {x, y, g11, g12, g22, w, wl, 0, ...}, G = F^-T F^-1 the metric
+// (|F^-1 d|^2 = d^T G d).  Staged in shared memory it is rewritten, per run,
+// into the bin-local expanded form of r^2 as a polynomial in the query point
+// q (coefficients duplicated for packed math):
+//   r^2 = e + g11 qx^2 + 2 g12 qx qy + g22 qy^2 + a qx + b qy,
+//   a = -2 (G c)_x, b = -2 (G c)_y, e = c^T G c   (c = local candidate position).
+struct __align__(16) CandF {
+    float f[16];
+};
+
 // Query record: wrapped position, output slot, image flags (16 bytes).
 struct QRec {
     float x, y;
@@ -64,7 +75,14 @@ enum EvalMode : int {
     EVAL_SPMV32 = 4,     // out_f64[id] = compensated FP32 sum
     EVAL_FIELD64 = 5,    // as FIELD, every pair in FP64 (weight w + wl), out_f64[id]
     EVAL_FIELD9_64 = 6,  // as FIELD9 in FP64
+    EVAL_FIELD_F = 7,    // as FIELD with deformed kernels W(|F^-1 d|) (CandF records)
+    EVAL_FIELD9_F = 8,   // as FIELD9 with deformed kernels
+    EVAL_FIELD_F_EXC = 9,// as FIELD_EXC with deformed kernels (pairs with |F^-1 d| < 1e-6 skipped)
 };
+
+__host__ __device__ constexpr bool eval_deformed(int mode) {
+    return mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F || mode == EVAL_FIELD_F_EXC;
+}
 
 enum SetMode : int {
     SET_SIGN_SPLIT = 0,  // set 0: omega > 0, set 1: omega < 0; weight |omega| * 2 sigma
@@ -81,6 +99,7 @@ struct InstDesc {
     float Lx, Ly, hw;
     int periodic;
     int p_begin, p_end;
+    float cover = 1.f;   // the walk covers cover * h_w: the largest stretch sigma_max(F) of a deformed kernel
 };
 
 // Plan the grid: fills `out` (n entries) and returns the bin count, or a
@@ -98,15 +117,18 @@ struct GridBufs {
     uint32_t* count = nullptr;  // nbins + 1
     uint32_t* start = nullptr;  // nbins + 1 (exclusive prefix, start[nbins] = candidates)
     Cand* cand = nullptr;       // n
+    CandF* candf = nullptr;     // n (deformed kernels only)
     uint32_t* perm = nullptr;   // n: sorted slot -> particle (points into rs buffers)
     RadixScratch rs{};
 };
-void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g);
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed = false);
 
 // Bin keys + counts + stable sort + ranges + gather.  weights == nullptr uses
 // omega (SET_SIGN_SPLIT scales |omega| by 2 sigma, SET_ONE_SIGNED by
-// 2 sigma too).  Writes g.cand / g.start / g.perm.
-int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode);
+// 2 sigma too).  Writes g.cand / g.start / g.perm; with F (per particle,
+// row-major {F11, F12, F21, F22}) it writes the deformed records g.candf.
+int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* omega, int set_mode,
+               const float4* F = nullptr);
 // Overwrite candidate weights from a vector in sorted order: cand[p].z/.w =
 // hi/lo FP32 split of scale * x[p] (FP64 in, for the SpMV).
 int grid_set_weights_sorted(vpmc_context* ctx, GridBufs& g, const double* x_sorted, double scale);
@@ -135,9 +157,11 @@ struct QueryBufs {
     uint32_t* qfill = nullptr;   // nbins
     uint32_t* qrank = nullptr;   // per point: rank inside its bin (from the counting atomic)
     QRec* qrec = nullptr;        // max points
+    uint4* tmp = nullptr;        // max points (two-pass placement of ranked points)
+    uint32_t* super_fill = nullptr;
     uint32_t* scan_tmp = nullptr;
 };
-void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q);
+void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool two_pass = false);
 // Bin arbitrary points (one instance `inst_of` lookup per point by index range
 // `point_inst` == nullptr -> instance 0).  set = candidate set to query.
 int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M, int set,
@@ -145,8 +169,13 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 // Scatter points whose bins are already in q.qbin (counts in q.qcount).
 int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M,
                    int field9);
-// Same, with each point's rank inside its bin already in q.qrank (no atomics).
+// Same, with each point's rank inside its bin already in q.qrank (no atomics;
+// through super-bins in two streaming passes when q.tmp is carved).
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M);
+
+// sigma_max over F[0..n) (+inf if some F is non-finite or has det <= 0);
+// d_words: 2 device words of scratch.  Synchronises the stream.
+int grid_max_sigma(vpmc_context* ctx, const float4* F, long n, unsigned* d_words, float* sigma);
 
 struct EvalLaunch {
     int mode = EVAL_FIELD;

@@ -160,6 +160,17 @@ __host__ __device__ __forceinline__ double spline_mass_d(double q) {
     return c * (0.06875 + g - 0.08125);
 }
 
+// Largest singular value of F = [[F.x, F.y], [F.z, F.w]]: the square root of
+// the largest eigenvalue of F^T F (how far a deformed kernel W(|F^-1 d|)
+// reaches, in units of h_w).
+__host__ __device__ __forceinline__ float sigma_max(float4 F) {
+    const double T = double(F.x) * F.x + double(F.y) * F.y + double(F.z) * F.z + double(F.w) * F.w;
+    const double d = double(F.x) * F.w - double(F.y) * F.z;
+    const double disc = T * T - 4.0 * d * d;
+    const double l = 0.5 * (T + sqrt(disc > 0.0 ? disc : 0.0));
+    return float(sqrt(l));
+}
+
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------------
 struct U4 { uint32_t x, y, z, w; };
 

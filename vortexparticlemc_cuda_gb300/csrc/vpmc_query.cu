@@ -92,13 +92,13 @@ struct Work {
 };
 
 int setup(vpmc_context* ctx, int slot, long N, float hw, float Lx, float Ly, int periodic, long M, int nvec,
-          Work* w, int k = 0) {
-    InstDesc d{Lx, Ly, hw, periodic, 0, int(N)};
+          Work* w, int k = 0, float cover = 1.f, bool deformed = false) {
+    InstDesc d{Lx, Ly, hw, periodic, 0, int(N), cover};
     const long nb = grid_plan(&d, 1, k, 1, &w->plan);
     if (nb < 0) return int(-nb);
     const long nq = M > N ? M : N;
     auto carve_all = [&](Carver& c) {
-        carve_grid(c, N, nb, 1, &w->g);
+        carve_grid(c, N, nb, 1, &w->g, deformed);
         carve_items(c, nb, nq, &w->it);
         if (M > 0) carve_queries(c, nb, M, &w->q);
         w->self = c.take<QRec>(size_t(N < 1 ? 1 : N));
@@ -146,21 +146,33 @@ int vpmc_query_vorticity(vpmc_context* ctx, int N, const float* pos, const float
                          float Ly, int periodic, float* out) {
     if (!ctx || N < 0 || M < 0 || !(h_w > 0.f) || !(Lx > 0.f) || !(Ly > 0.f)) return VPMC_ERR_INVALID;
     if ((N > 0 && (!pos || !omega)) || (M > 0 && (!pts || !out))) return VPMC_ERR_INVALID;
-    if (F) return VPMC_ERR_UNSUPPORTED;   // deformed kernels are not in this build
     VPMC_CUDA(cudaSetDevice(ctx->device));
     if (M == 0) return VPMC_OK;
     cudaStream_t st = ctx->stream;
     VPMC_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * size_t(M), st));
     if (N == 0) return vpmc_context_sync(ctx);
+    // deformed kernels: the walk must reach sigma_max(F) h_w (at most 2 h_w,
+    // the reach of the reference's 3x3 walk of 2 h_w cells)
+    float cover = 1.f;
+    if (F) {
+        char* sb = nullptr;
+        VPMC_TRY(scratch(ctx, SLOT_MISC, 64, &sb));
+        float sig = 1.f;
+        VPMC_TRY(grid_max_sigma(ctx, reinterpret_cast<const float4*>(F), N, reinterpret_cast<unsigned*>(sb), &sig));
+        if (!(sig <= 3.0e38f)) return VPMC_ERR_INVALID;   // non-finite F or det F <= 0
+        cover = sig > 1.f ? std::min(2.f, std::ceil(sig * 16.f) / 16.f) : 1.f;
+    }
     Work w;
-    VPMC_TRY(setup(ctx, SLOT_QUERY, N, h_w, Lx, Ly, periodic, M, 0, &w));
+    VPMC_TRY(setup(ctx, SLOT_QUERY, N, h_w, Lx, Ly, periodic, M, 0, &w, 0, cover, F != nullptr));
     const int set_mode = sign > 0 ? SET_POS_ONLY
                                    : (sign < 0 ? SET_NEG_ONLY : (use_signed ? SET_ONE_SIGNED : SET_ONE_ABS));
-    VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), omega, set_mode));
+    VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), omega, set_mode,
+                        reinterpret_cast<const float4*>(F)));
     VPMC_TRY(bin_points(ctx, w.g, w.q, reinterpret_cast<const float2*>(pts), M, 0, 0));
     VPMC_TRY(make_items(ctx, w.g, w.q.qstart, w.it, query_chunk(4)));
     EvalLaunch L;
-    L.mode = exclude_center ? EVAL_FIELD_EXC : EVAL_FIELD;
+    if (F) L.mode = exclude_center ? EVAL_FIELD_F_EXC : EVAL_FIELD_F;
+    else L.mode = exclude_center ? EVAL_FIELD_EXC : EVAL_FIELD;
     L.out_f32 = out;
     VPMC_TRY(launch_eval(ctx, w.g, w.q.qrec, w.it, L));
     if (sign < 0 && use_signed) VPMC_LAUNCH(k_scale_f32, blocks_for(M), 256, 0, st, out, long(M), -1.0f);

@@ -18,6 +18,14 @@
 //              a fixed order, u = u(+) - u(-), x += dt u with an FP64 wrap.
 //   Results do not depend on scheduling: each sample's field value is a fixed
 //   ordered sum and every reduction has a fixed tree.
+//
+// Deformation mode (the reference's step_cuda, which always runs with
+// aux = 1): every particle carries F (row-major float4); kernels are
+// W(|F^-1 d|), branch-1 jitter is F r, each target has four auxiliary points
+// x -/+ dx e_x, x +/- dx e_y (dx = h_w / 2) with their own disk samples and a
+// share of the branch-1 samples, and after the step F = renorm_det1(I + dt
+// grad u) from central differences of the auxiliary velocities
+// (update_jacobian_from5, src/cuda/monte_carlo_bs.cu:274-288).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -41,6 +49,7 @@ constexpr int kJitTab = 1024;     // inverse spline-radius CDF table (unbiased l
 
 struct InstMC {
     float Lx, Ly, hw, dt;
+    float dx;              // auxiliary-point offset, SimParam::dx = h_w / 2 (include/vortex_particle_mc.hpp:132)
     int periodic, law;
     float cum9[2];         // Omega_s (x9 when periodic), FP32 copy of the FP64 totals
     int cnt[2];
@@ -71,6 +80,21 @@ __host__ __device__ __forceinline__ float disk_radius(float2 d, bool periodic, f
             m = fmaxf(m, ex * ex + ey * ey);
         }
     return sqrtf(m);
+}
+
+// Cell-centred lattice, ix-major: x = (ix + 1/2) / Nx * Lx in FP64, rounded once.
+__global__ void k_lattice(float2* __restrict__ pos, int Nx, int Ny, float Lx, float Ly) {
+    const long n = long(Nx) * Ny;
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const long ix = i / Ny, iy = i - ix * Ny;
+        pos[i] = make_float2(float((double(ix) + 0.5) / double(Nx) * double(Lx)),
+                             float((double(iy) + 0.5) / double(Ny) * double(Ly)));
+    }
+}
+
+__global__ void k_identity(float4* __restrict__ F, long n) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+        F[i] = make_float4(1.f, 0.f, 0.f, 1.f);
 }
 
 // upper_bound(cdf[0..n), u) bracketed by a guide table of G = n entries:
@@ -107,7 +131,7 @@ struct GenArgs {
     int n_inst;
     const GridInst* gi;
     const float2* pos;
-    const float4* F;              // unused (F = I on this path)
+    const float4* F;              // deformation mode: per-particle F (branch-1 jitter F r); else nullptr
     const int* sub;
     const double* cdf;
     const uint32_t* guide;
@@ -115,14 +139,27 @@ struct GenArgs {
     const unsigned long long* step;
     long t0, nt;                  // target chunk
     int N1, N2;
+    int naux;                     // disk sample sets per target: 1, or 5 (C, L, R, T, B) in deformation mode
     float2* ys;
     uint32_t* qbin;
     uint32_t* qcount;
     uint32_t* qrank;
 };
 
+// Auxiliary point a of target x: C, L, R, T, B as monte_carlo_bs_kernel_safe
+// forms them (src/cuda/monte_carlo_bs.cu:163-167).
+__device__ __forceinline__ float2 aux_point(float2 x, int a, float dx) {
+    switch (a) {
+        case 1: return make_float2(x.x - dx, x.y);
+        case 2: return make_float2(x.x + dx, x.y);
+        case 3: return make_float2(x.x, x.y + dx);
+        case 4: return make_float2(x.x, x.y - dx);
+        default: return x;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
-    const int Q = a.N1 + a.N2;
+    const int Q = a.N1 + a.naux * a.N2;
     const long total = a.nt * 2 * Q;
     const unsigned long long step = *a.step;
     for (long sid = long(blockIdx.x) * blockDim.x + threadIdx.x; sid < total; sid += long(gridDim.x) * blockDim.x) {
@@ -171,18 +208,28 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                 }
                 float sn, cs;
                 sincosf(2.f * kPiF * u01(r.w), &sn, &cs);
-                y.x += rr * cs;
-                y.y += rr * sn;
+                const float jx = rr * cs, jy = rr * sn;
+                if (a.F) {
+                    // mul_mat2(F, r) (include/monte_carlo_bs.cuh:99-103)
+                    const float4 f = a.F[p];
+                    y.x += f.x * jx + f.y * jy;
+                    y.y += f.z * jx + f.w * jy;
+                } else {
+                    y.x += jx;
+                    y.y += jy;
+                }
             }
         } else {
-            const float R = disk_radius(x, I.periodic != 0, I.Lx, I.Ly);
+            const int ax = a.naux > 1 ? (j - a.N1) / a.N2 : 0;
+            const float2 xa = aux_point(x, ax, I.dx);
+            const float R = disk_radius(xa, I.periodic != 0, I.Lx, I.Ly);
             const float phi = 2.f * kPiF * u01(r.x);
             const float ur = u01(r.y);
             const float rr = I.law == VPMC_LAW_REFERENCE ? R * sqrtf(ur) : R * ur;
             float sn, cs;
             sincosf(phi, &sn, &cs);
-            y.x = x.x + rr * cs;
-            y.y = x.y + rr * sn;
+            y.x = xa.x + rr * cs;
+            y.y = xa.y + rr * sn;
         }
         uint32_t b = kNoBin;
         if (valid) {
@@ -297,6 +344,124 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
                     oy = float(ny);
                 }
                 a.pos_out[t] = make_float2(ox, oy);
+            }
+        }
+    }
+}
+
+// Deformation mode: one warp per target, five estimates (C, L, R, T, B).
+// Branch-1 samples serve all five points, disk samples j in
+// [N1 + a N2, N1 + (a+1) N2) serve point a; the normalisation is 1/(N1+N2)
+// for each.  Lane 0 writes u = u(+) - u(-) at C (and the four auxiliary
+// velocities), advects, and forms F_next = renorm_det1(I + dt grad u).
+struct Acc5Args {
+    const InstMC* mc;
+    int n_inst;
+    const float2* pos;
+    const float2* ys;
+    const float* fv;
+    long t0, nt;
+    int N1, N2;
+    int advect;
+    float2* vel;
+    float2* vel5;          // 5 per target
+    float2* pos_out;
+    float4* F_out;
+    unsigned* sig;         // [0] = max sigma_max(F_out) (float bits), [1] = targets with sigma_max > cap
+    float cap;
+};
+
+__global__ void __launch_bounds__(256) k_accum5(Acc5Args a) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
+    const int Q = a.N1 + 5 * a.N2;
+    const float w1 = float(a.N1) / float(a.N1 + a.N2), w2 = float(a.N2) / float(a.N1 + a.N2);
+    const float inv = 1.f / float(a.N1 + a.N2);
+    for (long tl = warp; tl < a.nt; tl += nwarps) {
+        const long t = a.t0 + tl;
+        const InstMC& I = a.mc[inst_of(a.mc, a.n_inst, t)];
+        const float2 x = a.pos[t];
+        float2 xa[5];
+        float R[5], alpha[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            xa[k] = aux_point(x, k, I.dx);
+            R[k] = disk_radius(xa[k], I.periodic != 0, I.Lx, I.Ly);
+            alpha[k] = 1.f / (2.f * kPiF * R[k]);
+        }
+        float u[5][2];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) u[k][0] = u[k][1] = 0.f;
+        for (int s = 0; s < 2; ++s) {
+            KSum sx[5], sy[5];
+            const long base = (tl * 2 + s) * Q;
+            for (int j = lane; j < a.N1; j += 32) {
+                const float2 y = a.ys[base + j];
+                const float f = a.fv[base + j];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    const float2 c = mis_term(I.law, xa[k], y, f, w1, w2, I.cum9[s], alpha[k], R[k], I);
+                    sx[k].add(c.x);
+                    sy[k].add(c.y);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const long b0 = base + a.N1 + long(k) * a.N2;
+                for (int j = lane; j < a.N2; j += 32) {
+                    const float2 c = mis_term(I.law, xa[k], a.ys[b0 + j], a.fv[b0 + j], w1, w2, I.cum9[s], alpha[k],
+                                              R[k], I);
+                    sx[k].add(c.x);
+                    sy[k].add(c.y);
+                }
+            }
+            const float sg = s == 0 ? 1.f : -1.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                u[k][0] += sg * (warp_sum_comp(sx[k].s, sx[k].c) * inv);
+                u[k][1] += sg * (warp_sum_comp(sy[k].s, sy[k].c) * inv);
+            }
+        }
+        if (lane == 0) {
+            const float vx = u[0][0], vy = u[0][1];
+            a.vel[t] = make_float2(vx, vy);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) a.vel5[5 * t + k] = make_float2(u[k][0], u[k][1]);
+            if (a.advect) {
+                double nx = double(x.x) + double(I.dt) * double(vx);
+                double ny = double(x.y) + double(I.dt) * double(vy);
+                float ox, oy;
+                if (I.periodic) {
+                    nx -= floor(nx / double(I.Lx)) * double(I.Lx);
+                    ny -= floor(ny / double(I.Ly)) * double(I.Ly);
+                    ox = float(nx);
+                    oy = float(ny);
+                    if (ox >= I.Lx) ox = 0.f;
+                    if (oy >= I.Ly) oy = 0.f;
+                } else {
+                    ox = float(nx);
+                    oy = float(ny);
+                }
+                a.pos_out[t] = make_float2(ox, oy);
+                // update_jacobian_from5 + renorm_det1 (src/cuda/monte_carlo_bs.cu:274-288,
+                // include/monte_carlo_bs.cuh:140-144), FP32 as there
+                const float c = 0.5f * I.dt / I.dx;
+                float4 F;
+                F.x = 1.f + (u[2][0] - u[1][0]) * c;
+                F.y = (u[3][0] - u[4][0]) * c;
+                F.z = (u[2][1] - u[1][1]) * c;
+                F.w = 1.f + (u[3][1] - u[4][1]) * c;
+                const float det = F.x * F.w - F.y * F.z;
+                const float sc = rsqrtf(fmaxf(det, 1e-12f));
+                F.x *= sc;
+                F.y *= sc;
+                F.z *= sc;
+                F.w *= sc;
+                a.F_out[t] = F;
+                const float sm = sigma_max(F);
+                atomicMax(&a.sig[0], __float_as_uint(sm));   // non-negative floats order as their bits
+                if (!(sm <= a.cap)) atomicAdd(&a.sig[1], 1u);
             }
         }
     }
@@ -505,7 +670,19 @@ struct vpmc_sim {
     float* fv = nullptr;
     double* fv64 = nullptr;            // FP64 path only
     double* cum64 = nullptr;           // per instance Omega_+-, x9 when periodic (FP64 path)
+    std::vector<double> cum64_h;       // host copy (the working set is re-carved on re-planning)
     int precision = 32;
+    // deformation mode
+    int deform = 0;
+    float cover = 1.f;                 // plan cover: sigma_max(F) the walk reaches
+    float min_cover = 1.f;
+    float sigma = 1.f;                 // sigma_max of the current F
+    long long over_cap = 0;            // particle-steps with sigma_max(F) > kCoverCap
+    float4* F = nullptr;
+    float4* F_next = nullptr;
+    unsigned* d_sig = nullptr;         // 2 words
+    DevBuf aux;                        // deformation mode: vel5 (kept across re-planning)
+    float2* vel5 = nullptr;            // 5 per particle
     long chunk_targets = 0;
     long max_samples = 0;
     // graphs
@@ -519,6 +696,17 @@ struct vpmc_sim {
 };
 
 namespace {
+
+constexpr float kCoverCap = 2.f;   // the reference's 3x3 walk of 2 h_w cells reaches 2 h_w
+
+// Samples per (target, sign): N1 branch-1 samples + N2 disk samples per point.
+long samples_per(const vpmc_sim* s) { return long(s->N1) + long(s->deform ? 5 : 1) * s->N2; }
+
+// Cover level for a stretch sigma: 1, else the next multiple of 1/16, at most kCoverCap.
+float cover_for(float sigma) {
+    if (!(sigma > 1.f)) return 1.f;
+    return std::min(kCoverCap, std::ceil(sigma * 16.f) / 16.f);
+}
 
 void drop_graphs(vpmc_sim* s) {
     if (s->graph_step) cudaGraphExecDestroy(s->graph_step);
@@ -558,11 +746,11 @@ int alloc_work(vpmc_sim* s) {
     std::vector<InstDesc> d(s->n_inst);
     for (int i = 0; i < s->n_inst; ++i)
         d[i] = InstDesc{s->prm[i].Lx, s->prm[i].Ly, s->mc[i].hw, s->prm[i].periodic, int(s->begin[i]),
-                        int(s->begin[i] + s->counts[i])};
+                        int(s->begin[i] + s->counts[i]), s->deform ? s->cover : 1.f};
     s->plan.resize(s->n_inst);
     const long nb = grid_plan(d.data(), s->n_inst, s->k_walk, 2, s->plan.data());
     if (nb < 0) return int(-nb);
-    const long Q2 = 2L * (s->N1 + s->N2);
+    const long Q2 = 2L * samples_per(s);
     long per_chunk = s->max_samples / Q2;
     if (per_chunk < 1) per_chunk = 1;
     if (per_chunk > s->N) per_chunk = s->N;
@@ -573,9 +761,9 @@ int alloc_work(vpmc_sim* s) {
     s->chunk_ev.assign(2 * nchunks, nullptr);
     for (auto& e : s->chunk_ev) VPMC_CUDA(cudaEventCreate(&e));
     auto carve_all = [&](Carver& c) {
-        carve_grid(c, s->N, nb, s->n_inst, &s->g);
+        carve_grid(c, s->N, nb, s->n_inst, &s->g, s->deform != 0);
         carve_items(c, nb, ns, &s->it);
-        carve_queries(c, nb, ns, &s->q);
+        carve_queries(c, nb, ns, &s->q, true);
         s->ys = c.take<float2>(size_t(ns));
         s->fv = c.take<float>(size_t(ns));
         s->fv64 = s->precision == 64 ? c.take<double>(size_t(ns)) : nullptr;
@@ -589,6 +777,39 @@ int alloc_work(vpmc_sim* s) {
     carve_all(c);
     VPMC_CUDA(cudaMemcpyAsync(s->g.inst, s->plan.data(), sizeof(GridInst) * s->plan.size(), cudaMemcpyHostToDevice,
                               ctx->stream));
+    if (!s->cum64_h.empty())
+        VPMC_CUDA(cudaMemcpyAsync(s->cum64, s->cum64_h.data(), sizeof(double) * s->cum64_h.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    return VPMC_OK;
+}
+
+// Deformation mode: read sigma_max of F (after a step from its F update,
+// else by a reduction over F) and re-plan the grid when the walk must reach
+// further.  reset = set the cover to what F needs (also lower); otherwise it
+// only grows.  Kernels stretched beyond kCoverCap are counted, not covered.
+// realloc: re-carve the working set even if the cover stays (mode switch).
+int refresh_cover(vpmc_sim* s, bool from_step, bool reset, bool realloc = false) {
+    cudaStream_t st = s->ctx->stream;
+    float sig = 1.f;
+    if (!from_step) {
+        VPMC_TRY(grid_max_sigma(s->ctx, s->F, s->N, s->d_sig, &sig));
+    } else {
+        unsigned h[2] = {0u, 0u};
+        VPMC_CUDA(cudaMemcpyAsync(h, s->d_sig, sizeof(h), cudaMemcpyDeviceToHost, st));
+        VPMC_CUDA(cudaStreamSynchronize(st));
+        std::memcpy(&sig, &h[0], sizeof(sig));
+        s->over_cap += h[1];
+    }
+    s->sigma = sig;
+    if (!s->deform) {
+        s->cover = 1.f;
+        if (realloc) VPMC_TRY(alloc_work(s));
+        return VPMC_OK;
+    }
+    const float need = std::max(s->min_cover, cover_for(sig));
+    const bool changed = reset ? need != s->cover : need > s->cover;
+    if (changed) s->cover = need;
+    if (changed || realloc) VPMC_TRY(alloc_work(s));
     return VPMC_OK;
 }
 
@@ -603,15 +824,17 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     VPMC_CUDA(cudaStreamIsCapturing(st, &cap));
     const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
-    VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
-    const int Q = s->N1 + s->N2;
+    const bool def = s->deform != 0;
+    VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT, def ? s->F : nullptr));
+    if (def && advect) VPMC_CUDA(cudaMemsetAsync(s->d_sig, 0, 2 * sizeof(unsigned), st));
+    const long Q = samples_per(s);
     float ms_total = 0.f;
     for (long t0 = 0; t0 < s->N; t0 += s->chunk_targets) {
         const long nt = std::min(s->chunk_targets, s->N - t0);
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
-        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
-                   nt, s->N1, s->N2, s->ys, s->q.qbin, s->q.qcount, s->q.qrank};
+        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, def ? s->F : nullptr, s->sub, s->cdf, s->guide, s->jit,
+                   s->d_step, t0, nt, s->N1, s->N2, def ? 5 : 1, s->ys, s->q.qbin, s->q.qcount, s->q.qrank};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
         VPMC_TRY(scatter_ranked(ctx, s->g, s->q, s->ys, ns));
         VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->precision == 64 ? 4 : s->qpt)));
@@ -620,7 +843,8 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         else VPMC_CUDA(cudaMemsetAsync(s->fv, 0, sizeof(float) * size_t(ns), st));
         EvalLaunch L;
         const bool unb = s->mc[0].law == VPMC_LAW_UNBIASED;
-        L.mode = f64 ? (unb ? EVAL_FIELD9_64 : EVAL_FIELD64) : (unb ? EVAL_FIELD9 : EVAL_FIELD);
+        L.mode = f64 ? (unb ? EVAL_FIELD9_64 : EVAL_FIELD64)
+                     : (def ? (unb ? EVAL_FIELD9_F : EVAL_FIELD_F) : (unb ? EVAL_FIELD9 : EVAL_FIELD));
         L.qpt = f64 ? 4 : s->qpt;
         L.out_f32 = s->fv;
         L.out_f64 = s->fv64;
@@ -628,7 +852,11 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, ev_flags));
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, ev_flags));
-        if (f64) {
+        if (def) {
+            Acc5Args aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
+                        s->vel5, s->pos_next, s->F_next, s->d_sig, kCoverCap};
+            VPMC_LAUNCH(k_accum5, blocks_for(nt * 32), 256, 0, st, aa);
+        } else if (f64) {
             AccArgs64 aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv64, s->cum64, t0, nt, s->N1, s->N2, advect ? 1 : 0,
                          s->vel, s->pos_next};
             VPMC_LAUNCH(k_accum64, blocks_for(nt * 32), 256, 0, st, aa);
@@ -640,6 +868,8 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     }
     if (advect) {
         VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+        if (def)
+            VPMC_CUDA(cudaMemcpyAsync(s->F, s->F_next, sizeof(float4) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
         VPMC_LAUNCH(k_inc_step, 1, 1, 0, st, s->d_step);
     }
     (void)ms_total;
@@ -739,6 +969,7 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
         // SimParam (include/vortex_particle_mc.hpp:119-133): h = Lx/Nx, h_w = h*hwr
         const float h = p.Lx / float(p.Nx);
         m.hw = h * p.hwr;
+        m.dx = 0.5f * m.hw;
         m.Lx = p.Lx;
         m.Ly = p.Ly;
         m.dt = p.dt;
@@ -765,6 +996,9 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
         s->jit = c.take<float>(kJitTab + 2);
         s->d_mc = c.take<InstMC>(size_t(n_inst));
         s->d_step = c.take<unsigned long long>(1);
+        s->F = c.take<float4>(size_t(N));
+        s->F_next = c.take<float4>(size_t(N));
+        s->d_sig = c.take<unsigned>(2);
     };
     carve_state(dry);
     int rc = s->mem.reserve(dry.off);
@@ -778,6 +1012,7 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
     cudaMemcpyAsync(s->jit, jt.data(), sizeof(float) * jt.size(), cudaMemcpyHostToDevice, st);
     unsigned long long zero = 0;
     cudaMemcpyAsync(s->d_step, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+    k_identity<<<blocks_for(N), 256, 0, st>>>(s->F, N);
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess) {
         vpmc_sim_destroy(s);
         return VPMC_ERR_CUDA;
@@ -799,6 +1034,7 @@ int vpmc_sim_destroy(vpmc_sim* s) {
     for (auto e : s->chunk_ev) if (e) cudaEventDestroy(e);
     s->mem.release();
     s->work.release();
+    s->aux.release();
     delete s;
     return VPMC_OK;
 }
@@ -874,6 +1110,7 @@ int vpmc_sim_prepare(vpmc_sim* s) {
         }
     }
     VPMC_TRY(upload_mc(s));
+    s->cum64_h = cum64_h;
     VPMC_CUDA(cudaMemcpyAsync(s->cum64, cum64_h.data(), sizeof(double) * cum64_h.size(), cudaMemcpyHostToDevice, st));
     VPMC_CUDA(cudaStreamSynchronize(st));
     drop_graphs(s);
@@ -917,7 +1154,10 @@ int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, i
 int vpmc_sim_step(vpmc_sim* s, int nsteps, int use_graph) {
     if (!s || nsteps < 0) return VPMC_ERR_INVALID;
     VPMC_CUDA(cudaSetDevice(s->ctx->device));
-    for (int k = 0; k < nsteps; ++k) VPMC_TRY(run_pass(s, true, use_graph));
+    for (int k = 0; k < nsteps; ++k) {
+        VPMC_TRY(run_pass(s, true, use_graph));
+        if (s->deform) VPMC_TRY(refresh_cover(s, true, false));
+    }
     VPMC_TRY(vpmc_context_sync(s->ctx));
     return collect_eval_time(s);
 }
@@ -941,6 +1181,7 @@ int vpmc_sim_step_host(vpmc_sim* s, const float* pos_in, float* pos_out, float* 
     cudaStream_t st = s->ctx->stream;
     if (pos_in) VPMC_CUDA(cudaMemcpyAsync(s->pos, pos_in, sizeof(float2) * size_t(s->N), cudaMemcpyHostToDevice, st));
     VPMC_TRY(run_pass(s, true, 1));
+    if (s->deform) VPMC_TRY(refresh_cover(s, true, false));
     if (pos_out) VPMC_CUDA(cudaMemcpyAsync(pos_out, s->pos, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToHost, st));
     if (vel_out) VPMC_CUDA(cudaMemcpyAsync(vel_out, s->vel, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToHost, st));
     return vpmc_context_sync(s->ctx);
@@ -975,6 +1216,7 @@ uint64_t vpmc_sim_get_step(vpmc_sim* s) { return s ? s->step : 0; }
 
 int vpmc_sim_set_precision(vpmc_sim* s, int bits) {
     if (!s || (bits != 32 && bits != 64)) return VPMC_ERR_INVALID;
+    if (bits == 64 && s->deform) return VPMC_ERR_UNSUPPORTED;   // deformed kernels run in FP32 only
     if (bits == s->precision) return VPMC_OK;
     s->precision = bits;
     VPMC_TRY(alloc_work(s));
@@ -1008,7 +1250,8 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
     if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
     const vpmc_sim_params& p = s->prm[0];
     const double density = double(s->counts[0]) / (double(p.Lx) * p.Ly) * double(s->mc[0].hw) * s->mc[0].hw;
-    const auto key = std::make_tuple(int(std::lround(p.hwr * 16)), s->N1 + s->N2, int(std::lround(density)));
+    const auto key = std::make_tuple(int(std::lround(p.hwr * 16 * (s->deform ? s->cover : 1.f))),
+                                     int(samples_per(s)) * (s->deform ? -1 : 1), int(std::lround(density)));
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -1070,8 +1313,123 @@ int vpmc_sim_geometry(vpmc_sim* s, long long* info) {
     info[3] = s->g.nbins;
     info[4] = s->plan.empty() ? 0 : s->plan[0].gx;
     info[5] = s->plan.empty() ? 0 : s->plan[0].k;
-    info[6] = 2LL * (s->N1 + s->N2);
+    info[6] = 2LL * samples_per(s);
     info[7] = s->eval_launches;
+    return VPMC_OK;
+}
+
+int vpmc_sim_reinit(vpmc_sim* s, double tol, int max_iter, double* info) {
+    if (!s || max_iter < 0) return VPMC_ERR_INVALID;
+    vpmc_context* ctx = s->ctx;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    for (int i = 0; i < s->n_inst; ++i) {
+        const vpmc_sim_params& p = s->prm[i];
+        // SimParam (include/vortex_particle_mc.hpp:119-133): Ny = round(Ly / h), h = Lx / Nx in FP32
+        const float h = p.Lx / float(p.Nx);
+        int Ny = int(std::round(p.Ly / h));
+        if (Ny == 0) Ny = 1;
+        if (long(p.Nx) * Ny != s->counts[i]) return VPMC_ERR_INVALID;
+    }
+    if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
+    int worst = VPMC_OK;
+    for (int i = 0; i < s->n_inst; ++i) {
+        const vpmc_sim_params& p = s->prm[i];
+        const long b = s->begin[i], n = s->counts[i];
+        if (n == 0) continue;
+        const float h = p.Lx / float(p.Nx);
+        const int Ny = std::max(1, int(std::round(p.Ly / h)));
+        // 1. the current field (signed, deformed kernels in deformation mode) at the new lattice
+        VPMC_LAUNCH(k_lattice, blocks_for(n), 256, 0, st, s->pos_next + b, p.Nx, Ny, p.Lx, p.Ly);
+        VPMC_TRY(vpmc_query_vorticity(ctx, int(n), reinterpret_cast<const float*>(s->pos + b), s->omega + b,
+                                      s->deform ? reinterpret_cast<const float*>(s->F + b) : nullptr, int(n),
+                                      reinterpret_cast<const float*>(s->pos_next + b), 0, 1, 0, s->mc[i].hw, p.Lx,
+                                      p.Ly, p.periodic, s->fv));
+        // 2. positions to the lattice, F to the identity
+        VPMC_CUDA(cudaMemcpyAsync(s->pos + b, s->pos_next + b, sizeof(float2) * size_t(n), cudaMemcpyDeviceToDevice,
+                                  st));
+        VPMC_LAUNCH(k_identity, blocks_for(n), 256, 0, st, s->F + b, n);
+        // 3. strengths re-fitted by CG-RBF
+        double inf[3] = {0, 0, 0};
+        const int rc = vpmc_cg_rbf(ctx, int(n), reinterpret_cast<const float*>(s->pos + b), s->fv, s->omega + b,
+                                   s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol, max_iter, inf);
+        if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) return rc;
+        if (rc != VPMC_OK) worst = rc;
+        if (info) { info[3 * i] = inf[0]; info[3 * i + 1] = inf[1]; info[3 * i + 2] = inf[2]; }
+    }
+    s->prepared = false;
+    VPMC_TRY(vpmc_sim_prepare(s));
+    if (s->deform) VPMC_TRY(refresh_cover(s, false, true));
+    VPMC_TRY(vpmc_context_sync(ctx));
+    return worst;
+}
+
+int vpmc_sim_vorticity_grid(vpmc_sim* s, int inst, int res_x, int res_y, int sign, float* out) {
+    if (!s || inst < 0 || inst >= s->n_inst || res_x < 1 || res_y < 1 || !out) return VPMC_ERR_INVALID;
+    if (long(res_x) * res_y > (1L << 28)) return VPMC_ERR_CAPACITY;
+    vpmc_context* ctx = s->ctx;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    const vpmc_sim_params& p = s->prm[inst];
+    const long b = s->begin[inst], n = s->counts[inst], m = long(res_x) * res_y;
+    char* base = nullptr;
+    VPMC_TRY(scratch(ctx, SLOT_DIRECT, sizeof(float2) * size_t(m) + 256, &base));
+    float2* pts = reinterpret_cast<float2*>(base);
+    VPMC_LAUNCH(k_lattice, blocks_for(m), 256, 0, ctx->stream, pts, res_x, res_y, p.Lx, p.Ly);
+    return vpmc_query_vorticity(ctx, int(n), reinterpret_cast<const float*>(s->pos + b), s->omega + b,
+                                s->deform ? reinterpret_cast<const float*>(s->F + b) : nullptr, int(m),
+                                reinterpret_cast<const float*>(pts), sign, sign == 0 ? 1 : 0, 0, s->mc[inst].hw,
+                                p.Lx, p.Ly, p.periodic, out);
+}
+
+int vpmc_sim_set_deformation(vpmc_sim* s, int on, float min_cover) {
+    if (!s || !(min_cover <= kCoverCap)) return VPMC_ERR_INVALID;
+    if (on && s->precision == 64) return VPMC_ERR_UNSUPPORTED;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    if (on && !s->vel5) {
+        VPMC_TRY(s->aux.reserve(5 * sizeof(float2) * size_t(s->N)));
+        s->vel5 = static_cast<float2*>(s->aux.p);
+        VPMC_CUDA(cudaMemsetAsync(s->vel5, 0, 5 * sizeof(float2) * size_t(s->N), s->ctx->stream));
+    }
+    s->deform = on ? 1 : 0;
+    s->min_cover = std::max(1.f, min_cover);
+    if (!s->deform) s->cover = 1.f;
+    VPMC_TRY(refresh_cover(s, false, true, true));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_set_F(vpmc_sim* s, const float* F, int is_host) {
+    if (!s || !F) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    VPMC_CUDA(cudaMemcpyAsync(s->F, F, sizeof(float4) * size_t(s->N),
+                              is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s->ctx->stream));
+    VPMC_TRY(refresh_cover(s, false, s->deform != 0));
+    if (!std::isfinite(s->sigma)) return VPMC_ERR_INVALID;   // non-finite or det <= 0 somewhere
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_get_F(vpmc_sim* s, float* F, int is_host) {
+    if (!s || !F) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    VPMC_CUDA(cudaMemcpyAsync(F, s->F, sizeof(float4) * size_t(s->N),
+                              is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s->ctx->stream));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_get_aux_velocities(vpmc_sim* s, float* vel5, int is_host) {
+    if (!s || !vel5) return VPMC_ERR_INVALID;
+    if (!s->deform || !s->vel5) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    VPMC_CUDA(cudaMemcpyAsync(vel5, s->vel5, 5 * sizeof(float2) * size_t(s->N),
+                              is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s->ctx->stream));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_deform_info(vpmc_sim* s, double* info) {
+    if (!s || !info) return VPMC_ERR_INVALID;
+    info[0] = s->sigma;
+    info[1] = s->deform ? s->cover : 1.0;
+    info[2] = double(s->over_cap);
+    info[3] = s->deform;
     return VPMC_OK;
 }
 

@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, SimParams, check, lib)
+from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, SimParams, VpmcError, check, lib)
 
 __all__ = [
     "fill_dummy", "Context", "context", "fill_cells", "counting_sort", "hash_build", "build_subsets",
@@ -177,10 +177,13 @@ def cubic_spline(r: float, h_w: float) -> float:
 # ---------------------------------------------------------- vorticity query (a7)
 def query_vorticity(pos, omega, pts, sign=1, use_signed=False, exclude_center=False, h_w=0.04, Lx=1.0, Ly=1.0,
                     periodic=True, F=None):
-    """queryVorticityAbs (include/vorticity_query.cuh:15-79) at every point of pts."""
+    """queryVorticityAbs (include/vorticity_query.cuh:15-79) at every point of pts.
+    F: (N, 4) row-major per-particle deformation (kernels W(|F^-1 d|)) or None."""
     pos = _cuda(pos, torch.float32, "pos", (2,))
     omega = _cuda(omega, torch.float32, "omega")
     pts = _cuda(pts, torch.float32, "pts", (2,))
+    if F is not None:
+        F = _cuda(F, torch.float32, "F", (4,))
     out = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
     check(lib().vpmc_query_vorticity(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(omega), _p(F), pts.shape[0],
                                      _p(pts), int(sign), int(use_signed), int(exclude_center), h_w, Lx, Ly,
@@ -228,6 +231,24 @@ def direct_velocity(pos, omega, kernel=DIRECT_MOLLIFIED, pts=None, tidx=None, pa
     check(lib().vpmc_direct_velocity_f64(context(_dev(pos)).h, kernel, pos.shape[0], _p(pos), _p(omega), m,
                                          _p(pts), _p(tidx), param, Lx, Ly, int(periodic), _p(out)),
           "vpmc_direct_velocity_f64")
+    return out
+
+
+def direct_velocity_f32(pos, omega, kernel=DIRECT_PLUMMER, pts=None, tidx=None, param=0.04, Lx=1.0, Ly=1.0,
+                        periodic=True):
+    """The deterministic "P" method: FP32 tiled direct sum -> (M, 2) float32."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    omega = _cuda(omega, torch.float32, "omega")
+    if kernel == DIRECT_PLUMMER:
+        tidx = _cuda(tidx, torch.int32, "tidx")
+        m = tidx.shape[0]
+    else:
+        pts = _cuda(pts, torch.float32, "pts", (2,))
+        m = pts.shape[0]
+    out = torch.empty((m, 2), dtype=torch.float32, device=pos.device)
+    check(lib().vpmc_direct_velocity_f32(context(_dev(pos)).h, kernel, pos.shape[0], _p(pos), _p(omega), m,
+                                         _p(pts), _p(tidx), param, Lx, Ly, int(periodic), _p(out)),
+          "vpmc_direct_velocity_f32")
     return out
 
 
@@ -374,10 +395,65 @@ class Simulation:
         keys = ("N", "chunk_targets", "chunks", "bins", "cells_x", "k_walk", "samples_per_target", "eval_launches")
         return dict(zip(keys, [int(v) for v in g]))
 
+    def reinit(self, tol: float = 1e-8, max_iter: int = 1000):
+        """Positions to the lattice, F = I, strengths re-fitted by CG to the
+        current field; returns per-instance CG info dicts."""
+        info = (C.c_double * (3 * len(self.counts)))()
+        rc = lib().vpmc_sim_reinit(self.h, float(tol), int(max_iter), C.cast(info, C.c_void_p))
+        if rc not in (0, 8):
+            check(rc, "vpmc_sim_reinit")
+        return [dict(iters=int(info[3 * i]), relres=info[3 * i + 1], true_relres=info[3 * i + 2])
+                for i in range(len(self.counts))]
+
+    def vorticity_grid(self, res_x: int, res_y: int | None = None, inst: int = 0, sign: int = 0):
+        """(res_x, res_y) field raster of instance inst (ix-major)."""
+        res_y = res_x if res_y is None else res_y
+        out = torch.empty((res_x, res_y), dtype=torch.float32, device=torch.device("cuda", self.ctx.device))
+        check(lib().vpmc_sim_vorticity_grid(self.h, int(inst), int(res_x), int(res_y), int(sign), _p(out)),
+              "vpmc_sim_vorticity_grid")
+        return out
+
+    # deformation mode (Simulation::step_cuda with aux = 1 and the F update)
+    def set_deformation(self, on: bool = True, min_cover: float = 0.0):
+        check(lib().vpmc_sim_set_deformation(self.h, int(bool(on)), float(min_cover)), "vpmc_sim_set_deformation")
+
+    def set_F(self, F):
+        F = _cuda(F, torch.float32, "F", (4,))
+        check(lib().vpmc_sim_set_F(self.h, _p(F), 0), "vpmc_sim_set_F")
+
+    def F(self):
+        out = torch.empty((self.N, 4), dtype=torch.float32, device=torch.device("cuda", self.ctx.device))
+        check(lib().vpmc_sim_get_F(self.h, _p(out), 0), "vpmc_sim_get_F")
+        return out
+
+    def aux_velocities(self):
+        """(N, 5, 2): u at C, L, R, T, B of the last pass (deformation mode)."""
+        out = torch.empty((self.N, 5, 2), dtype=torch.float32, device=torch.device("cuda", self.ctx.device))
+        check(lib().vpmc_sim_get_aux_velocities(self.h, _p(out), 0), "vpmc_sim_get_aux_velocities")
+        return out
+
+    def deform_info(self):
+        d = (C.c_double * 4)()
+        check(lib().vpmc_sim_deform_info(self.h, C.cast(d, C.c_void_p)), "vpmc_sim_deform_info")
+        return dict(sigma_max=d[0], cover=d[1], over_cap=int(d[2]), deformation=bool(d[3]))
+
     def last_stats(self):
         n, ms = C.c_int(), C.c_float()
         check(lib().vpmc_sim_last_stats(self.h, C.byref(n), C.byref(ms)), "vpmc_sim_last_stats")
         return dict(launches_per_step=n.value, eval_ms=ms.value)
+
+
+def write_pgm(path: str, field, lo: float | None = None, hi: float | None = None):
+    """Write a 2-D field (rows = y from top, columns = x) as an 8-bit PGM image
+    (the headless stand-in for the reference's PNG dump)."""
+    a = field.detach().cpu().numpy() if isinstance(field, torch.Tensor) else np.asarray(field)
+    img = np.flipud(a.T.astype(np.float64))
+    lo = float(img.min()) if lo is None else lo
+    hi = float(img.max()) if hi is None else hi
+    g = np.clip((img - lo) / (hi - lo if hi > lo else 1.0) * 255.0 + 0.5, 0, 255).astype(np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"P5\n%d %d\n255\n" % (g.shape[1], g.shape[0]))
+        f.write(g.tobytes())
 
 
 def philox4x32_10(ctr, key):
