@@ -320,6 +320,33 @@ int vpmc_sim_reinit(vpmc_sim* sim, double tol, int max_iter, double* info);
  * out: res_x * res_y floats (device). */
 int vpmc_sim_vorticity_grid(vpmc_sim* sim, int inst, int res_x, int res_y, int sign, float* out);
 
+/* ---------------------------------------------------------------- adjoint
+ * Gradients of a loss of the final positions with respect to the initial
+ * positions and the strengths, through nsteps plain-method MIS steps with
+ * the forward's own samples (common random numbers: the same Philox streams;
+ * the discrete CDF-index and image choices are held fixed, i.e. the pathwise
+ * derivative).  No counterpart in the reference.
+ *   vpmc_sim_record: run nsteps from the current state, keeping positions
+ *     every k_ckpt steps (and the final state) on the device.
+ *   vpmc_sim_adjoint: given dL/dX_T (2N doubles, device), recompute each
+ *     segment from its checkpoint and run the adjoint steps backwards; writes
+ *     dL/dX_0 (2N doubles) and dL/domega (N doubles); the simulation is left
+ *     in the recorded final state.  Field values, gradients and sums of the
+ *     adjoint are FP64; the trajectory is the forward's (its precision).
+ *     flags: VPMC_ADJ_SCORE adds the score-function term of the discrete
+ *     branch-1 draw (P(I = J) = |omega_J| / Omega), which makes dL/domega an
+ *     unbiased estimate of the gradient of the expected trajectory; without
+ *     it dL/domega is the exact derivative of the frozen-sampling estimator.
+ *   vpmc_sim_freeze_sampling: on = keep the |omega| CDF (sampling law) of
+ *     the last prepare when strengths change, refreshing only Omega; for
+ *     finite-difference checks of the pathwise derivative.  The sign of
+ *     every strength must stay (VPMC_ERR_INVALID otherwise).
+ * Deformation mode: VPMC_ERR_UNSUPPORTED. */
+int vpmc_sim_record(vpmc_sim* sim, int nsteps, int k_ckpt);
+enum { VPMC_ADJ_SCORE = 1 };
+int vpmc_sim_adjoint(vpmc_sim* sim, const double* dL_dXT, double* dL_dX0, double* dL_domega, int flags);
+int vpmc_sim_freeze_sampling(vpmc_sim* sim, int on);
+
 /* Change the estimator law / seed / step counter of an existing simulation. */
 int vpmc_sim_set_law(vpmc_sim* sim, int law);
 int vpmc_sim_set_seed(vpmc_sim* sim, uint64_t seed);

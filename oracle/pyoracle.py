@@ -25,7 +25,7 @@ __all__ = [
     "rcdf", "icdf", "spline_pdf", "spline_mass", "OracleState", "eval_vorticity_cpu",
     "query_vorticity_f64", "field_exact_f64", "mc_estimates", "mc_velocity", "mc_velocity_omp",
     "rbf_matvec_f64", "cg_rbf_f64", "direct_mollified_f64", "direct_plummer_f64", "direct_deformed_f64",
-    "mc_velocity5_omp",
+    "mc_velocity5_omp", "mis_forward_f64",
     "ref_available", "ref_fill_cells", "ref_counting_sort", "ref_build_subsets",
     "ref_rcdf", "ref_icdf", "ref_eval_vorticity", "ref_mc_estimates", "gaussian_field",
 ]
@@ -110,6 +110,8 @@ def lib():
             "orc_cg_rbf_f64": (ip, [vp, vp, vp, db, ip, db, ip, vp, vp, ip]),
             "orc_direct_mollified_f64": (None, [vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
             "orc_direct_deformed_f64": (None, [vp, vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
+            "orc_mis_forward_f64": (ip, [vp, vp, vp, ip, ip, fl, fl, fl, ip, ip, ip, ip, fl, C.c_uint64, C.c_uint64,
+                                         ip, vp, ip]),
             "orc_mc_velocity5_omp": (ip, [vp, vp, vp, vp, ip, ip, ip, fl, C.c_uint32, vp, ip, vp, ip]),
             "orc_direct_plummer_f64": (None, [vp, vp, ip, vp, ip, db, db, db, ip, vp, ip]),
             "orc_version": (C.c_char_p, []),
@@ -417,6 +419,22 @@ def mc_velocity5_omp(state: OracleState, targets, N1, N2, seed, nthreads=0):
                                     float(np.float32(0.5) * np.float32(state.prm.h_w)), seed, _ptr(vel), nthreads,
                                     _ptr(tab), len(tab))
     return vel, nt
+
+
+def mis_forward_f64(pos0, omega, prm: SimParam, law, seed, nsteps, step0=0, omega_sample=None, periodic=True,
+                    nthreads=0):
+    """nsteps of this build's MIS step in FP64 (frozen sampling law from
+    omega_sample, default omega); returns final positions (N, 2) float64."""
+    p = np.ascontiguousarray(pos0, np.float32)
+    w = np.ascontiguousarray(omega, np.float32)
+    ws = w if omega_sample is None else np.ascontiguousarray(omega_sample, np.float32)
+    out = np.zeros((len(p), 2), np.float64)
+    rc = lib().orc_mis_forward_f64(_ptr(p), _ptr(w), _ptr(ws), len(p), prm.Nx, prm.hwr, prm.Lx, prm.Ly,
+                                   int(periodic), int(law), prm.N1, prm.N2, prm.dt, int(seed), int(step0),
+                                   int(nsteps), _ptr(out), nthreads)
+    if rc != 0:
+        raise ValueError("omega and omega_sample differ in sign pattern")
+    return out
 
 
 def rbf_matvec_f64(state: OracleState, x, nthreads=0):

@@ -559,6 +559,202 @@ int orc_mc_velocity5_omp(const orc_mcctx* ctx, const float* pos, const float* F,
     return nt;
 }
 
+namespace {
+
+// ---- this build's MIS estimator restated in FP64 (for finite differences) ----
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the uniform maps the
+// product uses; key = mix32 of the seed, counter = (sample | sign << 31,
+// target, step lo, step hi).
+struct P4 { uint32_t x, y, z, w; };
+P4 philox(P4 c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c.x, p1 = uint64_t(0xCD9E8D57u) * c.z;
+        c = P4{uint32_t(p1 >> 32) ^ c.y ^ k0, uint32_t(p1), uint32_t(p0 >> 32) ^ c.w ^ k1, uint32_t(p0)};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+inline double u01f(uint32_t r) { return double((float(r >> 8) + 0.5f) * (1.0f / 16777216.0f)); }
+inline double u01dd(uint32_t r) { return (double(r) + 0.5) * (1.0 / 4294967296.0); }
+uint32_t mix32(uint64_t v) {
+    v ^= v >> 33;
+    v *= 0xff51afd7ed558ccdULL;
+    v ^= v >> 33;
+    v *= 0xc4ceb9fe1a85ec53ULL;
+    v ^= v >> 33;
+    return uint32_t(v);
+}
+
+}  // namespace
+
+int orc_mis_forward_f64(const float* pos0, const float* omega, const float* omega_sample, int N, int Nx,
+                        float hwr, float Lx, float Ly, int periodic, int law, int N1, int N2, float dt,
+                        uint64_t seed, uint64_t step0, int nsteps, double* pos_out, int nthreads) {
+    const int nt = threads_or_default(nthreads);
+    // SimParam: h = Lx / Nx, h_w = h * hwr in FP32
+    const float hf = Lx / float(Nx);
+    const double hw = double(hf * hwr);
+    const uint32_t k0 = mix32(seed * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL);
+    const uint32_t k1 = mix32(seed ^ 0xA4093822299F31D0ULL);
+    // sampling law (frozen): subsets and FP64 |omega| CDF of omega_sample
+    std::vector<int> sub[2];
+    std::vector<double> cdf[2];
+    for (int i = 0; i < N; ++i) {
+        const float w = omega_sample[i];
+        if (w == 0.f) continue;
+        const int s = w > 0.f ? 0 : 1;
+        sub[s].push_back(i);
+        cdf[s].push_back((cdf[s].empty() ? 0.0 : cdf[s].back()) + std::fabs(double(w)));
+    }
+    for (int s = 0; s < 2; ++s)
+        for (auto& c : cdf[s]) c /= cdf[s].back();
+    // Omega of the current strengths (x9 when periodic); the sign pattern must match
+    double cum[2] = {0.0, 0.0};
+    for (int i = 0; i < N; ++i) {
+        if ((omega[i] > 0.f) != (omega_sample[i] > 0.f) || (omega[i] < 0.f) != (omega_sample[i] < 0.f)) return -1;
+        if (omega[i] != 0.f) cum[omega[i] > 0.f ? 0 : 1] += std::fabs(double(omega[i]));
+    }
+    const double f9 = periodic ? 9.0 : 1.0;
+    // jitter tables: reference law = the reference's 20-entry iCDF, unbiased = inverse radial mass
+    float rc[20], icdf[20];
+    orc_build_cubic_rcdf(float(hw), 20, rc);
+    orc_cdf_to_icdf(rc, 20, float(hw), icdf);
+    std::vector<float> jit(1025);
+    for (int i = 0; i <= 1024; ++i) {
+        const double u = double(i) / 1024;
+        double lo = 0.0, hi = 1.0;
+        for (int it = 0; it < 80; ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (spline_mass_d(mid) < u) lo = mid; else hi = mid;
+        }
+        jit[i] = float(0.5 * (lo + hi));
+    }
+    jit[0] = 0.f;
+    jit[1024] = 1.f;
+    const int Q = N1 + N2;
+    const double w1 = double(N1) / Q, w2 = double(N2) / Q;
+    const double R = std::sqrt(double(Lx) * Lx + double(Ly) * Ly), alpha = 1.0 / (2.0 * kPiD * R);
+    const double sigma = 40.0 / (7.0 * kPiD * hw * hw);
+    std::vector<double> X(2 * size_t(N)), Xn(2 * size_t(N));
+    for (int i = 0; i < 2 * N; ++i) X[i] = pos0[i];
+    auto field = [&](int s, double yx, double yy) {
+        double f = 0.0;
+        const int lo = periodic ? -1 : 0, hi = periodic ? 1 : 0;
+        for (int J : sub[s]) {
+            const double aw = std::fabs(double(omega[J]));
+            for (int mx = lo; mx <= hi; ++mx)
+                for (int my = lo; my <= hi; ++my) {
+                    const double dx = yx - (X[2 * J] + mx * Lx), dy = yy - (X[2 * J + 1] + my * Ly);
+                    const double r = std::sqrt(dx * dx + dy * dy);
+                    if (r >= hw) continue;
+                    const double q = r / hw;
+                    f += aw * sigma * (q <= 0.5 ? 6.0 * (q * q * q - q * q) + 1.0 : 2.0 * (1 - q) * (1 - q) * (1 - q));
+                }
+        }
+        return f;
+    };
+    for (int n = 0; n < nsteps; ++n) {
+        const uint64_t step = step0 + uint64_t(n);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
+        for (int t = 0; t < N; ++t) {
+            const double x = X[2 * t], y0 = X[2 * t + 1];
+            double u[2] = {0.0, 0.0};
+            for (int s = 0; s < 2; ++s) {
+                const int ns = int(sub[s].size());
+                double ax = 0.0, ay = 0.0;
+                for (int j = 0; j < Q; ++j) {
+                    const P4 r = philox(P4{uint32_t(j) | (uint32_t(s) << 31), uint32_t(t), uint32_t(step),
+                                           uint32_t(step >> 32)}, k0, k1);
+                    double yx, yy;
+                    if (j < N1) {
+                        if (ns == 0) continue;
+                        const double uu = u01dd(r.x);
+                        int idx = int(std::upper_bound(cdf[s].begin(), cdf[s].end(), uu) - cdf[s].begin());
+                        idx = std::min(idx, ns - 1);
+                        const int p = sub[s][idx];
+                        yx = X[2 * p];
+                        yy = X[2 * p + 1];
+                        if (periodic) {
+                            const int m9 = std::min(int(float(u01f(r.y)) * 9.f), 8);
+                            yx += double(m9 / 3 - 1) * Lx;
+                            yy += double(m9 % 3 - 1) * Ly;
+                        }
+                        double rr;
+                        const float ur = float(u01f(r.z));
+                        if (law == 0) {
+                            const float f = ur * 19.f;
+                            const int i0 = int(f), i1 = std::min(i0 + 1, 19);
+                            const float tt = f - float(i0);
+                            rr = double(icdf[i0] * (1.f - tt) + icdf[i1] * tt) * hw;
+                        } else {
+                            const float f = ur * 1024.f;
+                            const int i0 = std::min(int(f), 1023);
+                            const float tt = f - float(i0);
+                            rr = double(jit[i0] * (1.f - tt) + jit[i0 + 1] * tt) * hw;
+                        }
+                        const double th = 2.0 * kPiD * u01f(r.w);
+                        yx += rr * std::cos(th);
+                        yy += rr * std::sin(th);
+                    } else {
+                        const double phi = 2.0 * kPiD * u01f(r.x), ur = u01f(r.y);
+                        const double rr = law == 0 ? R * std::sqrt(ur) : R * ur;
+                        yx = x + rr * std::cos(phi);
+                        yy = y0 + rr * std::sin(phi);
+                    }
+                    // field at the sample: unbiased law = the 3x3 images around the
+                    // sample's own tile; reference law = the periodic field
+                    double f = 0.0;
+                    if (periodic) {
+                        const double kx = std::floor(yx / Lx), ky = std::floor(yy / Ly);
+                        if (law == 1) {
+                            if (std::fabs(kx) > 2.0 || std::fabs(ky) > 2.0) continue;
+                            f = field(s, yx, yy);
+                        } else {
+                            f = field(s, yx - kx * Lx, yy - ky * Ly);
+                        }
+                    } else {
+                        if (yx < 0.0 || yx > Lx || yy < 0.0 || yy > Ly) continue;
+                        f = field(s, yx, yy);
+                    }
+                    if (!(f > 0.0)) continue;
+                    const double rx = x - yx, ry = y0 - yy;
+                    const double c = cum[s] * f9;
+                    double sc;
+                    if (law == 0) {
+                        double wx = rx, wy = ry;
+                        if (periodic) { wx = rx - std::round(rx / Lx) * Lx; wy = ry - std::round(ry / Ly) * Ly; }
+                        const double rn = std::max(std::sqrt(wx * wx + wy * wy), 1e-6);
+                        const double inv = 1.0 / (rx * rx + ry * ry + 1e-8);
+                        sc = f / (w1 * f / c + w2 * alpha / rn) * inv / (2.0 * kPiD);
+                    } else {
+                        const double r2 = rx * rx + ry * ry;
+                        if (!(r2 > 0.0)) continue;
+                        const double rn = std::sqrt(r2);
+                        const double p2 = rn < R ? alpha / rn : 0.0;
+                        sc = f / ((w1 * f / c + w2 * p2) * (2.0 * kPiD * r2));
+                    }
+                    ax += -ry * sc;
+                    ay += rx * sc;
+                }
+                const double sg = s == 0 ? 1.0 : -1.0;
+                u[0] += sg * ax / Q;
+                u[1] += sg * ay / Q;
+            }
+            double nx = x + double(dt) * u[0], ny = y0 + double(dt) * u[1];
+            if (periodic) {
+                nx -= std::floor(nx / Lx) * Lx;
+                ny -= std::floor(ny / Ly) * Ly;
+            }
+            Xn[2 * t] = nx;
+            Xn[2 * t + 1] = ny;
+        }
+        X.swap(Xn);
+    }
+    for (int i = 0; i < 2 * N; ++i) pos_out[i] = X[i];
+    return 0;
+}
+
 void orc_rbf_matvec_f64(const orc_view* all_view, const double* x, double* y,
                         double h_w, int periodic, int nthreads) {
     const orc_view& V = *all_view;

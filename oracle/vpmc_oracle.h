@@ -134,6 +134,18 @@ int  orc_mc_velocity5_omp(const orc_mcctx* ctx, const float* pos, const float* F
                           uint32_t seed, float* vel10, int nthreads, const float* icdf,
                           int icdf_L);
 
+/* This build's plain MIS step (both laws) restated in FP64 with FP64
+ * positions, for finite-difference checks of the adjoint: the library's
+ * Philox keys/counters and sampling maps, the branch-1 index drawn from the
+ * |omega| CDF of omega_sample (frozen sampling law) while field weights and
+ * Omega use omega, brute-force fields (3x3 images of the sample's tile for
+ * the unbiased law, the periodic field for the reference law), FP64 MIS
+ * terms, forward Euler with FP64 wrap.  law: 0 reference, 1 unbiased.
+ * Returns -1 if omega and omega_sample differ in sign pattern. */
+int orc_mis_forward_f64(const float* pos0, const float* omega, const float* omega_sample, int N, int Nx,
+                        float hwr, float Lx, float Ly, int periodic, int law, int N1, int N2, float dt,
+                        uint64_t seed, uint64_t step0, int nsteps, double* pos_out, int nthreads);
+
 /* ---- RBF system: src/cuda/cg_rbf_init.cu:11-116 restated in FP64 ---- */
 /* y = A x,  A_ij = W(|F_j^-1 (x_j - x_i)|) via the all-particle 3x3 walk. */
 void orc_rbf_matvec_f64(const orc_view* all_view, const double* x, double* y,

@@ -78,6 +78,9 @@ SIGNATURES = {
     "vpmc_sim_set_law": (_i, [_vp, _i]),
     "vpmc_sim_set_deformation": (_i, [_vp, _i, _f]),
     "vpmc_sim_reinit": (_i, [_vp, _d, _i, _vp]),
+    "vpmc_sim_record": (_i, [_vp, _i, _i]),
+    "vpmc_sim_adjoint": (_i, [_vp, _vp, _vp, _vp, _i]),
+    "vpmc_sim_freeze_sampling": (_i, [_vp, _i]),
     "vpmc_sim_vorticity_grid": (_i, [_vp, _i, _i, _i, _i, _vp]),
     "vpmc_sim_set_F": (_i, [_vp, _vp, _i]),
     "vpmc_sim_get_F": (_i, [_vp, _vp, _i]),

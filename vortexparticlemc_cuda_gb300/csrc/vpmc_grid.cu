@@ -456,6 +456,8 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
     constexpr bool kField64 = MODE == EVAL_FIELD64 || MODE == EVAL_FIELD9_64;
+    constexpr bool kGrad = eval_grad(MODE);
+    constexpr bool kDual9 = MODE == EVAL_DUAL9_64;
     constexpr bool kDef = eval_deformed(MODE);
     constexpr bool kDefExc = MODE == EVAL_FIELD_F_EXC;
     constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9 || MODE == EVAL_FIELD_F || MODE == EVAL_FIELD9_F;
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
     CandF* const s_candf = reinterpret_cast<CandF*>(s_cand);
     constexpr int NP = QPT / 2;   // packed query pairs
     static_assert(!kPacked || (QPT % 2 == 0), "packed path needs an even query count");
-    using Acc = typename std::conditional<kF64 || kField64, double, float>::type;
+    using Acc = typename std::conditional<kF64 || kField64 || kGrad, double, float>::type;
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -531,6 +533,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
         bool qv[QPT];
         Acc acc[QPT];
         float acc_c[QPT];
+        double accg[kGrad ? QPT : 1][2];
 #pragma unroll
         for (int j = 0; j < QPT; ++j) {
             const uint32_t idx = uint32_t(tid + j * kEvalThreads);
@@ -543,6 +546,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             qmy[j] = int((r.flags >> 3) & 7u) - 2;
             acc[j] = Acc(0);
             acc_c[j] = 0.f;
+            if constexpr (kGrad) accg[j][0] = accg[j][1] = 0.0;
         }
         __syncthreads();
 
@@ -700,6 +704,64 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                             part[j] = fmaf(cw, v, part[j]);
                         }
                     }
+                } else if constexpr (kGrad) {
+                    // FP64 value and gradient in q of sum w W(|q - c|):
+                    // dW/dr / r = 2 sigma (3 A r + 2 B) for r < h/2, -6 sigma t^2/(h r) below h
+                    const double hw = double(G.hw), ih = 1.0 / hw;
+                    const double A = 3.0 * ih * ih * ih, B = -3.0 * ih * ih;
+                    double px[QPT], py[QPT], pv[QPT], pgx[QPT], pgy[QPT];
+                    bool use[QPT];
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        px[j] = double(qx[j]) + double(pc.qdx);
+                        py[j] = double(qy[j]) + double(pc.qdy);
+                        pv[j] = pgx[j] = pgy[j] = 0.0;
+                        use[j] = true;
+                        if (MODE == EVAL_GRAD9_64) {
+                            const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
+                            use[j] = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
+                        }
+                    }
+                    for (int c = 0; c < cnt; ++c) {
+                        const Cand cv = cs[c];
+                        const double cxd = cv.x, cyd = cv.y, wd = double(cv.w) + double(cv.wl);
+                        bool cuse = true;
+                        if (kDual9) {
+                            // sample y with unwrapped tile k_y seen through image sxi of
+                            // this run: the source image it pairs with is k_y - sxi
+                            const uint32_t fl = __float_as_uint(cv.pad);
+                            const int mx = int(fl & 7u) - 2 - pc.mx, my = int((fl >> 3) & 7u) - 2 - pc.my;
+                            cuse = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
+                        }
+                        if (!cuse) continue;
+#pragma unroll
+                        for (int j = 0; j < QPT; ++j) {
+                            const double dx = px[j] - cxd, dy = py[j] - cyd;   // q - c
+                            const double r2 = dx * dx + dy * dy;
+                            const double r = sqrt(r2);
+                            if (r >= hw) continue;
+                            const double t = 1.0 - ih * r;
+                            double v, dr;   // W / 2 sigma and its r-derivative over r
+                            if (r <= 0.5 * hw) {
+                                v = 0.5 + r2 * (A * r + B);
+                                dr = 3.0 * A * r + 2.0 * B;
+                            } else {
+                                v = t * t * t;
+                                dr = -3.0 * t * t * ih / r;
+                            }
+                            pv[j] += wd * v;
+                            pgx[j] += wd * dr * dx;
+                            pgy[j] += wd * dr * dy;
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < QPT; ++j) {
+                        if (!use[j]) continue;
+                        acc[j] += pv[j];
+                        accg[j][0] += pgx[j];
+                        accg[j][1] += pgy[j];
+                        part[j] = 0.0;
+                    }
                 } else if constexpr (kField64) {
                     // the plain FP64 path: every pair and the sum in FP64
                     const double hw = double(G.hw), ih = 1.0 / hw;
@@ -775,7 +837,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                     }
                 }
 #pragma unroll
-                for (int j = 0; j < QPT; ++j) {
+                for (int j = 0; j < QPT && !kGrad; ++j) {
                     bool use = true;
                     if (kField9) {
                         const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
@@ -800,7 +862,11 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 #pragma unroll
         for (int j = 0; j < QPT; ++j) {
             if (!qv[j]) continue;
-            if constexpr (kF64 || kField64) a.out_f64[qid[j]] = acc[j];
+            if constexpr (kGrad) {
+                a.out_f64[3 * size_t(qid[j])] = acc[j];
+                a.out_f64[3 * size_t(qid[j]) + 1] = accg[j][0];
+                a.out_f64[3 * size_t(qid[j]) + 2] = accg[j][1];
+            } else if constexpr (kF64 || kField64) a.out_f64[qid[j]] = acc[j];
             else if constexpr (kComp) a.out_f64[qid[j]] = double(acc[j]) - double(acc_c[j]);
             else a.out_f32[qid[j]] = acc[j];
         }
@@ -1039,6 +1105,10 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
         case EVAL_FIELD_F_EXC:
             if (L.qpt != 4) return VPMC_ERR_INVALID;
             return launch_eval_t<EVAL_FIELD_F_EXC, 4>(ctx, a);
+        case EVAL_GRAD64: return launch_eval_t<EVAL_GRAD64, 4>(ctx, a);
+        case EVAL_GRAD9_64: return launch_eval_t<EVAL_GRAD9_64, 4>(ctx, a);
+        case EVAL_DUAL64: return launch_eval_t<EVAL_DUAL64, 4>(ctx, a);
+        case EVAL_DUAL9_64: return launch_eval_t<EVAL_DUAL9_64, 4>(ctx, a);
         case EVAL_FIELD64: return launch_eval_t<EVAL_FIELD64, 4>(ctx, a);
         case EVAL_FIELD9_64: return launch_eval_t<EVAL_FIELD9_64, 4>(ctx, a);
         default: return VPMC_ERR_INVALID;

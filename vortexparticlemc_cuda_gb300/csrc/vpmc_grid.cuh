@@ -78,7 +78,16 @@ enum EvalMode : int {
     EVAL_FIELD_F = 7,    // as FIELD with deformed kernels W(|F^-1 d|) (CandF records)
     EVAL_FIELD9_F = 8,   // as FIELD9 with deformed kernels
     EVAL_FIELD_F_EXC = 9,// as FIELD_EXC with deformed kernels (pairs with |F^-1 d| < 1e-6 skipped)
+    // FP64 value and gradient (adjoint): out_f64[3 id + {0, 1, 2}] = {f, df/dqx, df/dqy}
+    EVAL_GRAD64 = 10,    // f(q) = sum w W(|q - c|)
+    EVAL_GRAD9_64 = 11,  // same with the FIELD9 image mask of the query
+    EVAL_DUAL64 = 12,    // queries are particles, candidates are samples: G(q) = sum a_s W(|q - y_s|)
+    EVAL_DUAL9_64 = 13,  // same with each sample's FIELD9 image mask (flags in the candidate's pad word)
 };
+
+__host__ __device__ constexpr bool eval_grad(int mode) {
+    return mode == EVAL_GRAD64 || mode == EVAL_GRAD9_64 || mode == EVAL_DUAL64 || mode == EVAL_DUAL9_64;
+}
 
 __host__ __device__ constexpr bool eval_deformed(int mode) {
     return mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F || mode == EVAL_FIELD_F_EXC;

@@ -395,12 +395,30 @@ class Simulation:
         keys = ("N", "chunk_targets", "chunks", "bins", "cells_x", "k_walk", "samples_per_target", "eval_launches")
         return dict(zip(keys, [int(v) for v in g]))
 
+    # adjoint (common random numbers, checkpoints every k steps)
+    def record(self, nsteps: int, k_ckpt: int = 20):
+        check(lib().vpmc_sim_record(self.h, int(nsteps), int(k_ckpt)), "vpmc_sim_record")
+
+    def adjoint(self, dL_dXT, score: bool = False):
+        """dL/dX_T (N, 2) -> (dL/dX_0 (N, 2), dL/domega (N,)), float64 CUDA tensors.
+        score: add the score-function term of the discrete source draw
+        (unbiased gradient of the expected trajectory)."""
+        g = _cuda(dL_dXT.to(torch.float64), torch.float64, "dL_dXT", (2,))
+        dev = torch.device("cuda", self.ctx.device)
+        dx = torch.empty((self.N, 2), dtype=torch.float64, device=dev)
+        dw = torch.empty(self.N, dtype=torch.float64, device=dev)
+        check(lib().vpmc_sim_adjoint(self.h, _p(g), _p(dx), _p(dw), int(bool(score))), "vpmc_sim_adjoint")
+        return dx, dw
+
+    def freeze_sampling(self, on: bool = True):
+        check(lib().vpmc_sim_freeze_sampling(self.h, int(bool(on))), "vpmc_sim_freeze_sampling")
+
     def reinit(self, tol: float = 1e-8, max_iter: int = 1000):
         """Positions to the lattice, F = I, strengths re-fitted by CG to the
         current field; returns per-instance CG info dicts."""
         info = (C.c_double * (3 * len(self.counts)))()
         rc = lib().vpmc_sim_reinit(self.h, float(tol), int(max_iter), C.cast(info, C.c_void_p))
-        if rc not in (0, 8):
+        if rc not in (0, 9):   # VPMC_ERR_NOT_CONVERGED: the refit is still applied
             check(rc, "vpmc_sim_reinit")
         return [dict(iters=int(info[3 * i]), relres=info[3 * i + 1], true_relres=info[3 * i + 2])
                 for i in range(len(self.counts))]
@@ -441,6 +459,34 @@ class Simulation:
         n, ms = C.c_int(), C.c_float()
         check(lib().vpmc_sim_last_stats(self.h, C.byref(n), C.byref(ms)), "vpmc_sim_last_stats")
         return dict(launches_per_step=n.value, eval_ms=ms.value)
+
+
+class MCTrajectory(torch.autograd.Function):
+    """X_T = nsteps MIS steps of `sim` from (X_0, omega), differentiable in
+    X_0 and omega.  The backward pass is the library's hand-written adjoint
+    (vpmc_sim_adjoint) over the forward's own Philox samples, recomputing
+    segments from checkpoints every k_ckpt steps."""
+
+    @staticmethod
+    def forward(ctx, pos0, omega, sim, nsteps, k_ckpt, step0, score=False):
+        sim.set_particles(pos0.detach().float().contiguous(), omega.detach().float().contiguous())
+        sim.prepare()
+        sim.set_step(int(step0))
+        sim.record(int(nsteps), int(k_ckpt))
+        ctx.sim = sim
+        ctx.score = score
+        pos, _, _ = sim.particles()
+        return pos
+
+    @staticmethod
+    def backward(ctx, g):
+        dx, dw = ctx.sim.adjoint(g, ctx.score)
+        return dx.to(torch.float32), dw.to(torch.float32), None, None, None, None, None
+
+
+def trajectory(pos0, omega, sim, nsteps: int, k_ckpt: int = 20, step0: int = 0, score: bool = False):
+    """Differentiable final positions of `sim` (see MCTrajectory)."""
+    return MCTrajectory.apply(pos0, omega, sim, nsteps, k_ckpt, step0, score)
 
 
 def write_pgm(path: str, field, lo: float | None = None, hi: float | None = None):
