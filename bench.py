@@ -44,6 +44,8 @@ WORKLOADS = {
     "tg512": dict(Nx=512, hwr=16.0, N1=32, N2=32, dt=5e-4),
     "tg256": dict(Nx=256, hwr=8.0, N1=32, N2=32, dt=1e-3),
     "tg64": dict(Nx=64, hwr=4.0, N1=16, N2=16, dt=1e-3),
+    # 64 periodic instances, Nx from {96..384}, 8 Gaussian vortices each, one graph per step
+    "ens64": dict(Nx=0, hwr=8.0, N1=32, N2=32, dt=1e-3, ensemble=64),
 }
 
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -193,15 +195,25 @@ def strengths_cpu(wl, pos, b):
 
 def run_reference(args, wl):
     import oracle as O
+    from vortexparticlemc_cuda_gb300 import inputs as In
     rank = int(os.environ.get("RANK", "0"))
     if not reports(rank):
         return 0
-    pos = O.lattice(wl["Nx"])
-    b = O.taylor_green(pos)
-    # one CG iteration: on the lattice the Taylor-Green field is a single
-    # Fourier mode of the RBF matrix, so the first step already leaves only
-    # FP32 rounding of b; the timed estimator does not depend on the rest
-    omega, cg = strengths_cpu(wl, pos, b)
+    if wl.get("ensemble"):
+        # instance 0 of the ensemble; strengths = field x h^2 (the estimator's
+        # cost does not depend on the fitted values)
+        nxs, p_all, f_all = In.ensemble(wl["ensemble"])
+        wl = dict(wl, Nx=nxs[0])
+        pos = p_all[: nxs[0] ** 2]
+        omega = (f_all[: nxs[0] ** 2] / np.float32(nxs[0] ** 2)).astype(np.float32)
+        cg = {"iters": 0, "note": "strengths = field x h^2"}
+    else:
+        pos = In.lattice(wl["Nx"])
+        b = In.taylor_green(pos)
+        # one CG iteration: on the lattice the Taylor-Green field is a single
+        # Fourier mode of the RBF matrix, so the first step already leaves only
+        # FP32 rounding of b; the timed estimator does not depend on the rest
+        omega, cg = strengths_cpu(wl, pos, b)
     per_step_budget = max(1.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
     rate, nt, m, dt, st = cpu_reference_sample(wl, pos, omega, per_step_budget)
     times = []
@@ -233,7 +245,7 @@ def run_gpu(args, wl):
     import torch
     import torch.distributed as dist
 
-    import oracle as O
+    from vortexparticlemc_cuda_gb300 import inputs as In
     from vortexparticlemc_cuda_gb300 import phash as P
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -245,17 +257,31 @@ def run_gpu(args, wl):
     dev = torch.device("cuda", local)
 
     law = P.LAW_UNBIASED if args.law == "unbiased" else P.LAW_REFERENCE
-    pos = O.lattice(wl["Nx"])
+    ens = wl.get("ensemble", 0)
+    if ens:
+        nxs, pos, field = In.ensemble(ens)
+        counts = [nx * nx for nx in nxs]
+        sps = [P.SimParam(dt=wl["dt"], Nx=nx, hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law,
+                          seed=1000 * rank + i) for i, nx in enumerate(nxs)]
+    else:
+        nxs, pos, field = [wl["Nx"]], In.lattice(wl["Nx"]), None
+        counts = [len(pos)]
+        sps = [P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=rank)]
     N = len(pos)
-    sp = P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=rank)
-    sim = P.Simulation(sp, [N])
+    sp = sps[0]
+    sim = P.Simulation(sps, counts)
     tune = None
     pos_d = torch.from_numpy(pos).to(dev)
     sim.set_particles(pos_d, torch.zeros(N, device=dev))
     log = (lambda m: print(f"[bench {time.strftime('%H:%M:%S')}] {m}", file=sys.stderr, flush=True))  # noqa: E731
-    log(f"workload {args.workload}: N={N}, CG init (max {args.cg_iters} iterations)")
+    log(f"workload {args.workload}: N={N} in {len(counts)} instance(s), CG init (max {args.cg_iters} iterations)")
     t_cg = time.perf_counter()
-    cg = sim.init_strengths(None, tol=1e-8, max_iter=args.cg_iters)[0]
+    if ens:
+        infos = sim.init_strengths(torch.from_numpy(field).to(dev), tol=5e-3, max_iter=args.cg_iters)
+        cg = {"instances": len(infos), "max_true_relres": max(i["true_relres"] for i in infos),
+              "max_iters": max(i["iters"] for i in infos), "tol": 5e-3}
+    else:
+        cg = sim.init_strengths(None, tol=1e-8, max_iter=args.cg_iters)[0]
     t_cg = time.perf_counter() - t_cg
     _, omega_d, _ = sim.particles()
     log(f"CG done in {t_cg:.1f} s: {cg}")
@@ -264,18 +290,22 @@ def run_gpu(args, wl):
     # sum at 4096 random particles (seed 2)
     err = None
     if args.err_queries > 0:
-        idx = np.random.default_rng(2).choice(N, args.err_queries, replace=False)
+        n0 = counts[0]   # instance 0
+        idx = np.random.default_rng(2).choice(n0, min(args.err_queries, n0), replace=False)
         v0 = sim.velocity(step=0)
         q = pos_d[torch.from_numpy(idx).to(dev)]
-        truth = P.direct_velocity(pos_d, omega_d, P.DIRECT_MOLLIFIED, pts=q, param=sp.h_w).cpu().numpy()
+        truth = P.direct_velocity(pos_d[:n0], omega_d[:n0], P.DIRECT_MOLLIFIED, pts=q, param=sp.h_w).cpu().numpy()
         est = v0[torch.from_numpy(idx).to(dev)].cpu().numpy().astype(np.float64)
         rms = np.sqrt(np.mean(np.sum((est - truth) ** 2, 1)))
         ref = np.sqrt(np.mean(np.sum(truth ** 2, 1)))
-        p = pos[idx].astype(np.float64)
-        tg = np.stack([np.sin(2 * np.pi * p[:, 0]) * np.cos(2 * np.pi * p[:, 1]),
-                       -np.cos(2 * np.pi * p[:, 0]) * np.sin(2 * np.pi * p[:, 1])], 1)
-        err = {"vel_rel_rms_vs_fp64_direct": rms / ref, "queries": int(args.err_queries),
-               "direct_vs_taylor_green_rel_rms": float(np.sqrt(np.mean(np.sum((truth - tg) ** 2, 1))) / ref)}
+        err = {"vel_rel_rms_vs_fp64_direct": rms / ref, "queries": int(len(idx))}
+        if not ens:
+            p = pos[idx].astype(np.float64)
+            tg = np.stack([np.sin(2 * np.pi * p[:, 0]) * np.cos(2 * np.pi * p[:, 1]),
+                           -np.cos(2 * np.pi * p[:, 0]) * np.sin(2 * np.pi * p[:, 1])], 1)
+            err["direct_vs_taylor_green_rel_rms"] = float(np.sqrt(np.mean(np.sum((truth - tg) ** 2, 1))) / ref)
+        else:
+            err["instance"] = 0
 
     log(f"accuracy: {err}")
     if args.k or args.qpt:
@@ -354,7 +384,9 @@ def run_gpu(args, wl):
     log(f"e2e {e2e['value']:.3e} particle-steps/s")
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, nt, m, dt, _ = cpu_reference_sample(wl, pos, omega_d.cpu().numpy(), args.cpu_budget)
+        n0 = counts[0]   # an ensemble's baseline runs on instance 0
+        rate, nt, m, dt, _ = cpu_reference_sample(dict(wl, Nx=nxs[0]), pos[:n0], omega_d[:n0].cpu().numpy(),
+                                                  args.cpu_budget)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": nt, "kind": "port",
                "sample": f"{m} random targets ({dt:.1f} s), both signs, aux=0, Euler update, reference CPU "
                          f"estimator (monte_carlo_bs_cpu restated in oracle/, bit-exact), OpenMP over targets"}
@@ -363,11 +395,14 @@ def run_gpu(args, wl):
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (Taylor-Green lattice, strengths from CG-RBF)",
-        "config": {"workload": args.workload, **wl, "N": N, "law": args.law, "k_walk": geo["k_walk"],
+        "data": ("synthetic (64 Gaussian-vortex lattices, strengths from CG-RBF)" if ens
+                 else "synthetic (Taylor-Green lattice, strengths from CG-RBF)"),
+        "config": {"workload": args.workload, **wl, "N": N, "instances": len(counts),
+                   **({"Nx_per_instance": nxs} if ens else {}), "law": args.law, "k_walk": geo["k_walk"],
                    "cells_per_axis": geo["cells_x"], "chunks_per_step": geo["chunks"],
                    "queries_per_thread": sim.tuning()[1],
-                   "l2": "inputs larger than L2 (4.3 GB of sample records + 67 MB candidates per step)",
+                   "l2": f"inputs larger than L2 ({N * Q * 16 / 1e9:.1f} GB of sample records + "
+                         f"{N * 32 / 1e6:.0f} MB candidates per step)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": roof,
         "cpu_baseline": cpu,

@@ -149,6 +149,8 @@ def test_autograd_function_returns_adjoint(cuda):
     sim.record(5, 2)
     xt2 = sim.particles()[0]
     assert torch.equal(xt.detach(), xt2)
-    dx, dw = sim.adjoint(2.0 * (xt2.double() - 0.5))
-    assert torch.allclose(p0.grad.double(), dx, rtol=1e-6, atol=1e-9 * dx.abs().max().item())
-    assert torch.allclose(w0.grad.double(), dw, rtol=1e-6, atol=1e-9 * dw.abs().max().item())
+    dx, dw = sim.adjoint((2.0 * (xt.detach() - target)).double())   # the float32 gradient autograd passes
+    # the autograd path returns them as float32 (the leaves' dtype)
+    for got, want in ((p0.grad.double(), dx), (w0.grad.double(), dw)):
+        err = ((got - want).abs() / (want.abs() + 1e-6 * want.abs().max())).max().item()
+        assert err < 1e-5, err
