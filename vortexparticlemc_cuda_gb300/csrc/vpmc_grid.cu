@@ -12,7 +12,7 @@ namespace vpmc {
 namespace {
 
 constexpr int kEvalThreads = 256;
-constexpr int kMaxK = 4;
+constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
 constexpr int kCandCap = 1664;                 // candidates staged per batch (52 KB: 4 CTAs per SM)
 constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
@@ -215,10 +215,12 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 // super-bin (one global atomic per CTA and super-bin), pass 2 streams the
 // super-bin segments and writes each record to its final slot -- a region
 // the size of one super-bin at a time, which stays in L2 until it is full.
-constexpr int kCoarseTile = 16;   // samples per thread per tile
+constexpr int kCoarseTile = 8;        // samples per thread per tile
+constexpr int kCoarseThreads = 512;   // 4096 samples per tile: runs of ~16 records per super-bin
 constexpr int kMaxSuper = 2048;
+constexpr int kTargetSuper = 256;     // super-bins per grid: a super-bin's records (~33 MB at 2^29 samples) stay in L2
 
-__global__ void __launch_bounds__(256) k_scatter_coarse(const float2* __restrict__ pts, long M,
+__global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
                                                          const GridInst* __restrict__ inst, int n_inst,
                                                          const uint32_t* __restrict__ qbin,
                                                          const uint32_t* __restrict__ qrank,
@@ -509,7 +511,13 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 } else if (gxx < 0 || gxx >= G.gx) {
                     continue;
                 }
-                const int ylo = cy - G.k, yhi = cy + G.k;
+                // rows of this column that can hold a candidate within reach
+                // (reach <= k s): cell (ox, oy) is at least
+                // s sqrt((|ox|-1)^2 + (|oy|-1)^2) from every point of the bin's cell
+                const int ax = abs(ox) > 0 ? abs(ox) - 1 : 0;
+                int m = G.k;
+                while (m > 1 && ax * ax + (m - 1) * (m - 1) >= G.k * G.k) --m;
+                const int ylo = cy - m, yhi = cy + m;
                 if (G.periodic) {
                     if (ylo < 0) { add(gxx, 0, yhi, sxi, 0); add(gxx, ylo + G.gy, G.gy - 1, sxi, -1); }
                     else if (yhi >= G.gy) { add(gxx, ylo, G.gy - 1, sxi, 0); add(gxx, 0, yhi - G.gy, sxi, 1); }
@@ -1054,14 +1062,14 @@ int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
     VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
     if (q.tmp && M <= (1L << 29)) {   // sample ids and slots fit 29 bits
         int shift = 0;
-        while (((g.nbins - 1) >> shift) + 1 > kMaxSuper / 2) ++shift;
+        while (((g.nbins - 1) >> shift) + 1 > kTargetSuper) ++shift;
         const int nsuper = int(((g.nbins - 1) >> shift) + 1);
         cudaStream_t st = ctx->stream;
         VPMC_CUDA(cudaMemsetAsync(q.super_fill, 0, sizeof(uint32_t) * size_t(nsuper), st));
-        const long tiles = (M + kCoarseTile * 256 - 1) / (kCoarseTile * 256);
+        const long tiles = (M + long(kCoarseTile) * kCoarseThreads - 1) / (long(kCoarseTile) * kCoarseThreads);
         const int grid = int(std::min<long>(tiles, 8L * ctx->sm_count));
-        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), 256, 0, st, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,
-                    q.qstart, shift, nsuper, q.super_fill, q.tmp);
+        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), kCoarseThreads, 0, st, pts, M, g.inst, g.n_inst, q.qbin,
+                    q.qrank, q.qstart, shift, nsuper, q.super_fill, q.tmp);
         VPMC_LAUNCH(k_scatter_fine, blocks_for(M), 256, 0, st, q.tmp, q.qstart + g.nbins, M, q.qrec);
         return VPMC_OK;
     }
