@@ -212,16 +212,16 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 // different DRAM sector per sample (the bins of consecutive samples are
 // unrelated), so the placement goes through coarse super-bins (2^S
 // consecutive bins): pass 1 moves each CTA's tile of samples into runs per
-// super-bin (one global atomic per CTA and super-bin), pass 2 streams the
-// super-bin segments and writes each record to its final slot -- a region
-// the size of one super-bin at a time, which stays in L2 until it is full.
-constexpr int kCoarseTile = 8;        // samples per thread per tile
-constexpr int kCoarseThreads = 512;   // 4096 samples per tile: runs of ~16 records per super-bin
+// super-bin (one global atomic per CTA and super-bin) as {unwrapped point,
+// sample id, final slot}, pass 2 streams the super-bin segments, wraps each
+// point (deriving its image flags) and writes the record to its final slot
+// -- a region the size of one super-bin at a time, which stays in L2.
+constexpr int kCoarseTile = 16;       // samples per thread per tile
+constexpr int kCoarseThreads = 256;   // 4096 samples per tile
 constexpr int kMaxSuper = 2048;
-constexpr int kTargetSuper = 256;     // super-bins per grid: a super-bin's records (~33 MB at 2^29 samples) stay in L2
+constexpr int kTargetSuper = 1024;    // super-bins per grid: one super-bin region at a time stays in L2
 
 __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
-                                                         const GridInst* __restrict__ inst, int n_inst,
                                                          const uint32_t* __restrict__ qbin,
                                                          const uint32_t* __restrict__ qrank,
                                                          const uint32_t* __restrict__ qstart, int shift, int nsuper,
@@ -255,31 +255,31 @@ __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2*
             if (sb[j] == kNoBin) continue;
             const long m = t0 + long(j) * blockDim.x + threadIdx.x;
             const uint32_t b = qbin[m];
-            const GridInst& G = inst[inst_of_bin(inst, n_inst, b)];
-            float2 p = pts[m];
-            uint32_t ikx = 2u, iky = 2u;
-            if (G.periodic) {
-                const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
-                p.x = p.x - kx * G.Lx;
-                p.y = p.y - ky * G.Ly;
-                ikx = uint32_t(min(max(int(kx), -2), 2) + 2);
-                iky = uint32_t(min(max(int(ky), -2), 2) + 2);
-            }
-            const uint32_t slot = qstart[b] + qrank[m];
-            tmp[hist[sb[j]] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y),
-                                                  uint32_t(m) | (ikx << 29), slot | (iky << 29));
+            const float2 p = pts[m];   // unwrapped: pass 2 wraps it and derives the image flags
+            tmp[hist[sb[j]] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), uint32_t(m),
+                                                  qstart[b] + qrank[m]);
         }
         __syncthreads();
     }
 }
 
 __global__ void k_scatter_fine(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total, long M,
+                               const uint32_t* __restrict__ qbin, const GridInst* __restrict__ inst, int n_inst,
                                QRec* __restrict__ qrec) {
     const long n = min(long(*total), M);
-    constexpr uint32_t low = (1u << 29) - 1u;
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
         const uint4 r = tmp[i];
-        qrec[r.w & low] = QRec{__uint_as_float(r.x), __uint_as_float(r.y), r.z & low, (r.z >> 29) | ((r.w >> 29) << 3)};
+        float2 p = make_float2(__uint_as_float(r.x), __uint_as_float(r.y));
+        const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, qbin[r.z])];
+        uint32_t fl = (2u) | (2u << 3);
+        if (G.periodic) {
+            const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+            p.x = p.x - kx * G.Lx;
+            p.y = p.y - ky * G.Ly;
+            const int ikx = min(max(int(kx), -2), 2), iky = min(max(int(ky), -2), 2);
+            fl = uint32_t(ikx + 2) | (uint32_t(iky + 2) << 3);
+        }
+        qrec[r.w] = QRec{p.x, p.y, r.z, fl};
     }
 }
 
@@ -1060,7 +1060,7 @@ int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
 
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M) {
     VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
-    if (q.tmp && M <= (1L << 29)) {   // sample ids and slots fit 29 bits
+    if (q.tmp && M < (1L << 32)) {
         int shift = 0;
         while (((g.nbins - 1) >> shift) + 1 > kTargetSuper) ++shift;
         const int nsuper = int(((g.nbins - 1) >> shift) + 1);
@@ -1068,9 +1068,10 @@ int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
         VPMC_CUDA(cudaMemsetAsync(q.super_fill, 0, sizeof(uint32_t) * size_t(nsuper), st));
         const long tiles = (M + long(kCoarseTile) * kCoarseThreads - 1) / (long(kCoarseTile) * kCoarseThreads);
         const int grid = int(std::min<long>(tiles, 8L * ctx->sm_count));
-        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), kCoarseThreads, 0, st, pts, M, g.inst, g.n_inst, q.qbin,
-                    q.qrank, q.qstart, shift, nsuper, q.super_fill, q.tmp);
-        VPMC_LAUNCH(k_scatter_fine, blocks_for(M), 256, 0, st, q.tmp, q.qstart + g.nbins, M, q.qrec);
+        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), kCoarseThreads, 0, st, pts, M, q.qbin, q.qrank, q.qstart,
+                    shift, nsuper, q.super_fill, q.tmp);
+        VPMC_LAUNCH(k_scatter_fine, blocks_for(M), 256, 0, st, q.tmp, q.qstart + g.nbins, M, q.qbin, g.inst,
+                    g.n_inst, q.qrec);
         return VPMC_OK;
     }
     VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, ctx->stream, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,

@@ -1281,7 +1281,7 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
     s->N = N;
     s->N1 = prms[0].N1;
     s->N2 = prms[0].N2;
-    s->max_samples = 1L << 29;   // sample records per chunk (32 B each): fuller bins, fewer passes
+    s->max_samples = 1L << 30;   // samples per chunk (~52 B of records each): fuller bins, fewer passes
     long b = 0;
     s->mc.resize(n_inst);
     for (int i = 0; i < n_inst; ++i) {
