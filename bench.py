@@ -285,6 +285,9 @@ def run_gpu(args, wl):
     t_cg = time.perf_counter() - t_cg
     _, omega_d, _ = sim.particles()
     log(f"CG done in {t_cg:.1f} s: {cg}")
+    if args.deform:
+        # the reference's step_cuda: deformed kernels, 5-point auxiliary targets, F update
+        sim.set_deformation(True)
 
     # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
     # sum at 4096 random particles (seed 2)
@@ -361,7 +364,7 @@ def run_gpu(args, wl):
 
     # roofline of the dominant kernel (field evaluation, FP32-pipe bound)
     peaks, peak_kind = measured_peaks()
-    Q = 2 * (wl["N1"] + wl["N2"])
+    Q = 2 * (wl["N1"] + (5 if args.deform else 1) * wl["N2"])
     n_hit = np.pi * wl["hwr"] ** 2 / 2.0            # same-sign particles within h_w (TG: half of them)
     launches = max(1, geo["chunks"])
     eval_ms_launch = float(np.mean(eval_ms)) / launches
@@ -371,11 +374,12 @@ def run_gpu(args, wl):
     fp32_peak = sm_count * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     achieved = flop_launch / (eval_ms_launch / 1e3) / 1e12
     clocks = clk.summary()
-    roof = {"bound": "fp32", "kernel": "k_eval (field evaluation at MIS samples)",
+    roof = {"bound": "fp32", "kernel": ("k_eval, deformed kernels" if args.deform else "k_eval") +
+                                       " (field evaluation at MIS samples)",
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
             "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
                            f"({peak_kind}); no tensor-core or HBM bound applies (H3)",
-            "traffic": profile_traffic(args.workload),
+            "traffic": None if args.deform else profile_traffic(args.workload),
             "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.0f} in-support pairs x 16 flop",
             "eval_ms_per_launch": eval_ms_launch, "eval_share_of_step": float(np.mean(eval_ms)) / (ms / args.steps)}
     if clocks.get("sm_mhz"):
@@ -398,7 +402,8 @@ def run_gpu(args, wl):
         "data": ("synthetic (64 Gaussian-vortex lattices, strengths from CG-RBF)" if ens
                  else "synthetic (Taylor-Green lattice, strengths from CG-RBF)"),
         "config": {"workload": args.workload, **wl, "N": N, "instances": len(counts),
-                   **({"Nx_per_instance": nxs} if ens else {}), "law": args.law, "k_walk": geo["k_walk"],
+                   **({"Nx_per_instance": nxs} if ens else {}), "law": args.law,
+                   "method": "deformation (aux = 1, F update)" if args.deform else "plain", "k_walk": geo["k_walk"],
                    "cells_per_axis": geo["cells_x"], "chunks_per_step": geo["chunks"],
                    "queries_per_thread": sim.tuning()[1],
                    "l2": f"inputs larger than L2 ({N * Q * 16 / 1e9:.1f} GB of sample records + "
@@ -436,6 +441,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--deform", action="store_true",
+                    help="time the deformation step (the reference's step_cuda with aux = 1) instead of the plain one")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

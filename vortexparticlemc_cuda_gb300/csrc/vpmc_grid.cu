@@ -633,8 +633,18 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             for (int b = 0; b < nbp; ++b) {
                 const BatchPiece bp = s_bp[b];
                 const Piece pc = s_pc[bp.piece];
+                int cnt = int(bp.cnt);
+                if constexpr (kPacked) {
+                    // staged runs sit back to back in shared memory, already in the
+                    // bin's frame: consecutive runs under the same image mask are one sweep
+                    while (b + 1 < nbp) {
+                        const Piece nx = s_pc[s_bp[b + 1].piece];
+                        if (kField9 && (nx.mx != pc.mx || nx.my != pc.my)) break;
+                        cnt += int(s_bp[b + 1].cnt);
+                        ++b;
+                    }
+                }
                 const Cand* cs = s_cand + bp.soff;
-                const int cnt = int(bp.cnt);
                 Acc part[QPT];
                 if constexpr (kPacked && kDef) {
                     // queries in the local frame: the monomials of the expanded metric form
