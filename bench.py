@@ -288,6 +288,9 @@ def run_gpu(args, wl):
     if args.deform:
         # the reference's step_cuda: deformed kernels, 5-point auxiliary targets, F update
         sim.set_deformation(True)
+    if args.precision == 64:
+        # the plain FP64 GPU path of the same estimator (the spec comparison baseline)
+        sim.set_precision(64)
 
     # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
     # sum at 4096 random particles (seed 2)
@@ -311,8 +314,8 @@ def run_gpu(args, wl):
             err["instance"] = 0
 
     log(f"accuracy: {err}")
-    if args.k or args.qpt:
-        sim.set_tuning(args.k, args.qpt)
+    if args.k or args.qpt or args.precision == 64:
+        sim.set_tuning(args.k or 4, args.qpt or 4)   # FP64: no autotuning passes (seconds each)
     else:
         t_t = time.perf_counter()
         k_sel, q_sel, best = sim.autotune()
@@ -398,7 +401,7 @@ def run_gpu(args, wl):
     out = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32",
+        "vs_baseline": None, "dtype": "f64" if args.precision == 64 else "f32",
         "data": ("synthetic (64 Gaussian-vortex lattices, strengths from CG-RBF)" if ens
                  else "synthetic (Taylor-Green lattice, strengths from CG-RBF)"),
         "config": {"workload": args.workload, **wl, "N": N, "instances": len(counts),
@@ -441,6 +444,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", type=int, choices=[32, 64], default=32,
+                    help="64: the plain FP64 path (field values, MIS terms, sums in FP64)")
     ap.add_argument("--deform", action="store_true",
                     help="time the deformation step (the reference's step_cuda with aux = 1) instead of the plain one")
     args = ap.parse_args()

@@ -292,6 +292,15 @@ int vpmc_advect(vpmc_context* ctx, int N, float* pos, const float* vel, const do
  * reach of the reference's 3x3 walk of 2 h_w cells); min_cover (<= 2) forces
  * a wider reach.  FP32 only (VPMC_ERR_UNSUPPORTED with precision 64). */
 int vpmc_sim_set_deformation(vpmc_sim* sim, int on, float min_cover);
+/* update_jacobian_from5 + renorm_det1 (src/cuda/monte_carlo_bs.cu:274-288,
+ * include/monte_carlo_bs.cuh:140-150) for callers that hold the five velocity
+ * arrays (float2, device; velC is not read, as in the reference): F_out
+ * (float4, device) = renorm_det1(I + dt grad u) with grad u from central
+ * differences of L/R/T/B at offset dx, in FP32 as the reference. */
+int vpmc_update_jacobian_from5(vpmc_context* ctx, int N, float dt, float dx, const float* velC,
+                               const float* velL, const float* velR, const float* velT,
+                               const float* velB, float* F_out);
+
 /* F of every particle (4N floats); set_F rejects det F <= 0 or non-finite F. */
 int vpmc_sim_set_F(vpmc_sim* sim, const float* F, int is_host);
 int vpmc_sim_get_F(vpmc_sim* sim, float* F, int is_host);

@@ -95,6 +95,14 @@ int main(int argc, char** argv) {
         dump("vel1", sim.particles_.vel.to_host());
         dump("F1", sim.particles_.F.to_host());
 
+        {   // the reference's kernels as host calls: biot_savart_naive_kernel
+            dvec<float2> u{size_t(N)};
+            biot_savart_naive(sim.particles_.d_p(), sim.particles_.d_omega(), N, raw_ptr(u), P.Lx, P.Ly, true,
+                              0.5f * P.h_w);
+            dump("naive_pos", sim.particles_.pos.to_host());
+            dump("naive_u", u.to_host());
+        }
+
         std::vector<float2> before = sim.particles_.pos.to_host();
         sim.step_cuda_naive(true);
         dump("pos_naive_before", before);

@@ -77,6 +77,11 @@ def test_matvec_step_and_naive_step(run):
     w = (w - np.floor(w)).astype(np.float32)
     w[w >= 1] = 0
     assert np.array_equal(p1, w)
+    # biot_savart_naive (host call of the FP32 "P" kernel) against the FP64 Plummer sum
+    npos = run("naive_pos", np.float32).reshape(-1, 2)
+    nu = run("naive_u", np.float32).reshape(-1, 2)
+    want_u = O.direct_plummer_f64(npos, omega, np.arange(len(npos), dtype=np.int32), 0.5 * prm.h_w)
+    assert np.abs(nu - want_u).max() <= 1e-4 * np.abs(want_u).max()
     pb, pa = run("pos_naive_before", np.float32).reshape(-1, 2), run("pos_naive_after", np.float32).reshape(-1, 2)
     u = O.direct_plummer_f64(pb, omega, np.arange(len(pb), dtype=np.int32), 0.5 * prm.h_w)
     w = pb.astype(np.float64) + np.float64(np.float32(1e-3)) * u

@@ -183,3 +183,28 @@ def test_deformation_rejects_fp64_and_bad_F(cuda):
     bad = np.tile(np.array([1, 1, 1, 1], np.float32), (len(pos), 1))     # det 0
     with pytest.raises(P.VpmcError):
         sim.set_F(to_dev(bad, cuda))
+
+
+def test_update_jacobian_from5_abi(cuda):
+    """vpmc_update_jacobian_from5: the reference's FP32 renorm_det1(I + dt grad u)."""
+    import ctypes as C
+
+    import torch
+
+    from vortexparticlemc_cuda_gb300 import phash as P
+    from vortexparticlemc_cuda_gb300._lib import check, lib
+    rng = np.random.default_rng(2)
+    n, dt, dx = 5000, np.float32(1e-3), np.float32(0.01)
+    v = [rng.normal(size=(n, 2)).astype(np.float32) for _ in range(5)]
+    dv = [to_dev(a, cuda) for a in v]
+    F = torch.empty((n, 4), dtype=torch.float32, device=cuda)
+    ptr = lambda t: C.c_void_p(t.data_ptr())   # noqa: E731
+    check(lib().vpmc_update_jacobian_from5(P.context(0).h, n, float(dt), float(dx), *[ptr(t) for t in dv], ptr(F)),
+          "vpmc_update_jacobian_from5")
+    c = np.float32(np.float32(0.5) * dt) / dx
+    uL, uR, uT, uB = v[1], v[2], v[3], v[4]
+    f = np.stack([np.float32(1) + (uR[:, 0] - uL[:, 0]) * c, (uT[:, 0] - uB[:, 0]) * c,
+                  (uR[:, 1] - uL[:, 1]) * c, np.float32(1) + (uT[:, 1] - uB[:, 1]) * c], 1).astype(np.float32)
+    det = (f[:, 0] * f[:, 3] - f[:, 1] * f[:, 2]).astype(np.float32)
+    want = f / np.sqrt(np.maximum(det, np.float32(1e-12)))[:, None]
+    assert np.abs(F.cpu().numpy() - want).max() <= 2e-6

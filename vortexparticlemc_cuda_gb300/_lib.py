@@ -77,6 +77,7 @@ SIGNATURES = {
     "vpmc_advect": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i]),
     "vpmc_sim_set_law": (_i, [_vp, _i]),
     "vpmc_sim_set_deformation": (_i, [_vp, _i, _f]),
+    "vpmc_update_jacobian_from5": (_i, [_vp, _i, _f, _f, _vp, _vp, _vp, _vp, _vp, _vp]),
     "vpmc_sim_reinit": (_i, [_vp, _d, _i, _vp]),
     "vpmc_sim_record": (_i, [_vp, _i, _i]),
     "vpmc_sim_adjoint": (_i, [_vp, _vp, _vp, _vp, _i]),

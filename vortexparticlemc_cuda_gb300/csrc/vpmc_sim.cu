@@ -82,6 +82,26 @@ __host__ __device__ __forceinline__ float disk_radius(float2 d, bool periodic, f
     return sqrtf(m);
 }
 
+// update_jacobian_from5 + renorm_det1 (src/cuda/monte_carlo_bs.cu:274-288,
+// include/monte_carlo_bs.cuh:140-144) for callers that hold the five velocity
+// arrays themselves; the same FP32 steps as the deformation step.
+__global__ void k_jacobian5(long n, float dt, float dx, const float2* __restrict__ vC, const float2* __restrict__ vL,
+                            const float2* __restrict__ vR, const float2* __restrict__ vT,
+                            const float2* __restrict__ vB, float4* __restrict__ F) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        (void)vC;
+        const float c = 0.5f * dt / dx;
+        float4 f;
+        f.x = 1.f + (vR[i].x - vL[i].x) * c;
+        f.y = (vT[i].x - vB[i].x) * c;
+        f.z = (vR[i].y - vL[i].y) * c;
+        f.w = 1.f + (vT[i].y - vB[i].y) * c;
+        const float det = f.x * f.w - f.y * f.z;
+        const float sc = rsqrtf(fmaxf(det, 1e-12f));
+        F[i] = make_float4(f.x * sc, f.y * sc, f.z * sc, f.w * sc);
+    }
+}
+
 // Cell-centred lattice, ix-major: x = (ix + 1/2) / Nx * Lx in FP64, rounded once.
 __global__ void k_lattice(float2* __restrict__ pos, int Nx, int Ny, float Lx, float Ly) {
     const long n = long(Nx) * Ny;
@@ -1657,6 +1677,19 @@ int vpmc_sim_geometry(vpmc_sim* s, long long* info) {
     info[6] = 2LL * samples_per(s);
     info[7] = s->eval_launches;
     return VPMC_OK;
+}
+
+int vpmc_update_jacobian_from5(vpmc_context* ctx, int N, float dt, float dx, const float* velC, const float* velL,
+                                const float* velR, const float* velT, const float* velB, float* F_out) {
+    if (!ctx || N < 0 || !(dx > 0.f)) return VPMC_ERR_INVALID;
+    if (N == 0) return VPMC_OK;
+    if (!velL || !velR || !velT || !velB || !F_out) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    VPMC_LAUNCH(k_jacobian5, blocks_for(N), 256, 0, ctx->stream, long(N), dt, dx,
+                reinterpret_cast<const float2*>(velC), reinterpret_cast<const float2*>(velL),
+                reinterpret_cast<const float2*>(velR), reinterpret_cast<const float2*>(velT),
+                reinterpret_cast<const float2*>(velB), reinterpret_cast<float4*>(F_out));
+    return vpmc_context_sync(ctx);
 }
 
 int vpmc_sim_reinit(vpmc_sim* s, double tol, int max_iter, double* info) {
