@@ -25,34 +25,40 @@ def _minimg(d):
     return d - np.round(d)
 
 
-def _sim(cuda, law, Nx=24, hwr=4, N1=8, N2=8, dt=2e-3, seed=3, precision=64):
+def _sim(cuda, law, Nx=24, hwr=4, N1=8, N2=8, dt=2e-3, seed=3, precision=64, periodic=True):
     from vortexparticlemc_cuda_gb300 import phash as P
     pos = O.lattice(Nx)
     prm = O.SimParam(dt=dt, Nx=Nx, hwr=hwr, N1=N1, N2=N2)
     rng = np.random.default_rng(1)
     om = (O.taylor_green(pos) * np.float32(prm.h * prm.h) * (1 + 0.2 * rng.random(len(pos)))).astype(np.float32)
-    sim = P.Simulation(P.SimParam(dt=dt, Nx=Nx, hwr=hwr, N1=N1, N2=N2, law=law, seed=seed), [len(pos)])
+    sim = P.Simulation(P.SimParam(dt=dt, Nx=Nx, hwr=hwr, N1=N1, N2=N2, law=law, seed=seed, periodic=periodic),
+                       [len(pos)])
     sim.set_precision(precision)
     sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
     sim.prepare()
     return sim, pos, om, prm
 
 
-@pytest.mark.parametrize("law", [0, 1])
-def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law):
+@pytest.mark.parametrize("law,periodic", [(0, True), (1, True), (1, False)])
+def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law, periodic):
     T, K, seed = 6, 4, 3
-    sim, pos, om, prm = _sim(cuda, law, seed=seed)
+    sim, pos, om, prm = _sim(cuda, law, seed=seed, periodic=periodic)
     sim.freeze_sampling(True)
     rng = np.random.default_rng(7)
-    base = O.mis_forward_f64(pos, om, prm, law, seed, T)
+    fwd = lambda p, w, **kw: O.mis_forward_f64(p, w, prm, law, seed, T, periodic=periodic, **kw)   # noqa: E731
+    base = fwd(pos, om)
     xref = base + 0.01 * rng.normal(size=base.shape)
-    loss = lambda X: float(np.sum(_minimg(X - xref) ** 2))   # noqa: E731
+    if periodic:
+        loss = lambda X: float(np.sum(_minimg(X - xref) ** 2))   # noqa: E731
+    else:
+        loss = lambda X: float(np.sum((X - xref) ** 2))   # noqa: E731
 
     sim.set_step(0)
     sim.record(T, K)
     xt = sim.particles()[0].cpu().numpy().astype(np.float64)
-    assert np.abs(_minimg(xt - base)).max() < 1e-5          # the GPU trajectory is the oracle's
-    g = torch.from_numpy(2.0 * _minimg(xt - xref)).to(cuda)
+    d = _minimg(xt - base) if periodic else xt - base
+    assert np.abs(d).max() < 1e-5                            # the GPU trajectory is the oracle's
+    g = torch.from_numpy(2.0 * (_minimg(xt - xref) if periodic else xt - xref)).to(cuda)
     dx0, dw = (t.cpu().numpy() for t in sim.adjoint(g))
 
     idx = rng.choice(len(pos), 32, replace=False)
@@ -62,8 +68,8 @@ def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law):
         op, omn = om.copy(), om.copy()
         op[j] = np.float32(om[j] + eps)
         omn[j] = np.float32(om[j] - eps)
-        lp = loss(O.mis_forward_f64(pos, op, prm, law, seed, T, omega_sample=om))
-        lm = loss(O.mis_forward_f64(pos, omn, prm, law, seed, T, omega_sample=om))
+        lp = loss(fwd(pos, op, omega_sample=om))
+        lm = loss(fwd(pos, omn, omega_sample=om))
         fd.append((lp - lm) / (float(op[j]) - float(omn[j])))
     fd = np.array(fd)
     assert np.linalg.norm(dw[idx] - fd) <= 1e-4 * np.linalg.norm(fd), (dw[idx][:6], fd[:6])
@@ -76,8 +82,8 @@ def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law):
             pp, pm = pos.copy(), pos.copy()
             pp[t, c] = np.float32(pos[t, c] + 1e-5)
             pm[t, c] = np.float32(pos[t, c] - 1e-5)
-            lp = loss(O.mis_forward_f64(pp, om, prm, law, seed, T))
-            lm = loss(O.mis_forward_f64(pm, om, prm, law, seed, T))
+            lp = loss(fwd(pp, om))
+            lm = loss(fwd(pm, om))
             fdx.append((lp - lm) / (float(pp[t, c]) - float(pm[t, c])))
     fdx = np.array(fdx)
     got = dx0[pidx].reshape(-1)

@@ -84,6 +84,21 @@ def test_deformed_query_matches_fp64_oracle(cuda):
     assert np.abs(got.cpu().numpy() - want).max() <= 1e-5 * np.abs(want).max()
 
 
+def test_deformed_query_non_periodic(cuda):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    prm = O.SimParam(dt=1e-3, Nx=48, hwr=4, N1=16, N2=16)
+    pos = O.lattice(48)
+    rng = np.random.default_rng(9)
+    om = rng.normal(size=len(pos)).astype(np.float32)
+    F = random_F(len(pos), 0.1, 6)
+    st = O.OracleState(pos, om, prm, F=F)
+    pts = (rng.random((2000, 2)) * 1.1 - 0.05).astype(np.float32)   # some outside the domain
+    got = P.query_vorticity(to_dev(pos, cuda), to_dev(om, cuda), to_dev(pts, cuda), sign=1, h_w=prm.h_w,
+                            periodic=False, F=to_dev(F, cuda)).cpu().numpy()
+    want = O.query_vorticity_f64(st.view("pos"), pts, 1, False, False, prm.h_w, False)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
 def test_identity_F_reproduces_plain_velocity(cuda):
     for law in (0, 1):
         plain, pos, om, prm = _setup(cuda, law=law, deform=False)

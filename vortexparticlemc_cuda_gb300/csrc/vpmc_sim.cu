@@ -1625,7 +1625,7 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
         }
     }
     cudaStream_t st = s->ctx->stream;
-    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {2, 8}, {3, 8}};
+    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {2, 8}, {3, 8}, {4, 8}};
     float best = 1e30f;
     int bk = 0, bq = 4;
     for (const auto& c : cands) {
