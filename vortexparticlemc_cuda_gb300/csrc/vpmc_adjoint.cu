@@ -1,0 +1,395 @@
+// vpmc_adjoint.cu -- the adjoint of the plain MIS step (no counterpart in
+// the reference): checkpointed forward record, segment recompute, and per
+// step the FP64 value/gradient field sums at the samples, the per-sample
+// derivatives of the MIS term, and the transposed field sum at the particles.
+#include <algorithm>
+#include <vector>
+
+#include "vpmc_sim.cuh"
+
+namespace vpmc {
+namespace {
+
+using namespace sim;
+
+// ------------------------------------------------------------------ adjoint
+// The adjoint of one plain MIS step X' = X + dt U(X, omega) with the step's
+// Philox samples held fixed (common random numbers; the discrete CDF index
+// and image-tile choices are constants of the pathwise derivative).  With
+// lambda' = dL/dX' and v_t = dt lambda'_t (+-1/Q per sign), each MIS term
+// T(x_t, y, f(y), Omega) contributes c = v_t . T and
+//   dL/dx_t   += dc/dx                       (and dc/dy for disk samples, y = x_t + offset)
+//   dL/dx_I   += dc/dy                       (branch-1 samples, y = x_I + shift + F r)
+//   dc/dy      = -dc/dx|_f + dc/df grad f(y)
+//   dL/domega_J, dL/dx_J through f(y) = sum_J |omega_J| W(|y - x_J|):
+//              sgn(omega_J) G(x_J) and |omega_J| grad G(x_J), G(q) = sum_s dc_s/df W(|q - y_s|)
+//              (the transposed field sum, evaluated with queries and candidates swapped)
+//   dL/domega_J through Omega: sgn(omega_J) (9 if periodic) sum_s dc_s/dOmega.
+
+// d(v . T)/d{x, f, Omega} of one MIS term in FP64 (mis_term64's arithmetic).
+__device__ __forceinline__ void mis_term_adj(int law, float2 xf, float2 yf, double f, double w1, double w2,
+                                             double cum, double alpha, double R, const InstMC& I, double vx,
+                                             double vy, double& gxx, double& gxy, double& df, double& dc,
+                                             double& cval) {
+    gxx = gxy = df = dc = cval = 0.0;
+    if (!(f > 0.0)) return;
+    const double rx = double(xf.x) - double(yf.x), ry = double(xf.y) - double(yf.y);
+    const double P = vy * rx - vx * ry;   // v . perp(r)
+    if (law == VPMC_LAW_REFERENCE) {
+        double wx = rx, wy = ry;
+        if (I.periodic) {
+            wx = rx - round(rx / I.Lx) * I.Lx;
+            wy = ry - round(ry / I.Ly) * I.Ly;
+        }
+        const double wn = sqrt(wx * wx + wy * wy);
+        const double rn = fmax(wn, 1e-6);
+        const double inv = 1.0 / (rx * rx + ry * ry + 1e-8);
+        const double K = inv / (2.0 * kPiD);
+        const double denom = w1 * f / cum + w2 * alpha / rn;
+        const double sc = f / denom;
+        const double drx = wn > 1e-6 ? wx / wn : 0.0, dry = wn > 1e-6 ? wy / wn : 0.0;   // d rn / d r
+        const double g = sc / denom * (w2 * alpha / (rn * rn));                          // d sc / d rn
+        cval = sc * K * P;
+        gxx = sc * K * vy - 2.0 * rx * inv * K * sc * P + K * P * g * drx;
+        gxy = -sc * K * vx - 2.0 * ry * inv * K * sc * P + K * P * g * dry;
+        df = K * P * (1.0 - f * w1 / (cum * denom)) / denom;
+        dc = K * P * sc * (w1 * f / (cum * cum * denom));
+        return;
+    }
+    const double r2 = rx * rx + ry * ry;
+    if (!(r2 > 0.0)) return;
+    const double rn = sqrt(r2);
+    const bool in = rn < R;
+    const double p2 = in ? alpha / rn : 0.0;
+    const double D = w1 * f / cum + w2 * p2;
+    const double sc = f / (D * 2.0 * kPiD * r2);
+    const double ex = (in ? -w2 * alpha / (rn * r2) : 0.0) / D + 2.0 / r2;   // -(d sc / d r) / (sc r)
+    cval = sc * P;
+    gxx = sc * vy - P * sc * ex * rx;
+    gxy = -sc * vx - P * sc * ex * ry;
+    df = P * (1.0 - f * w1 / (cum * D)) / (2.0 * kPiD * r2 * D);
+    dc = P * sc * (w1 * f / (cum * cum * D));
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct AdjArgs {
+    const InstMC* mc;
+    int n_inst;
+    const float2* pos;
+    const float2* ys;
+    const double* fg;       // 3 per sample: f, df/dx, df/dy
+    const int* src;
+    const double* cum64;    // 2 per instance (x9 when periodic)
+    long t0, nt;
+    int N1, N2;
+    const double* lam_next;
+    double* lam;
+    double* as;             // per sample: dc/df
+    double* dcum;           // 2 per instance
+    double* gsc;            // score-function term: per particle, sum of c over the samples that drew it
+    double* csum;           // 2 per instance: sum of c over branch-1 samples
+};
+
+// One warp per target: the MIS-term derivatives of all its samples.
+__global__ void __launch_bounds__(256) k_adj_terms(AdjArgs a) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
+    const int Q = a.N1 + a.N2;
+    const double w1 = double(a.N1) / Q, w2 = double(a.N2) / Q, inv = 1.0 / Q;
+    for (long tl = warp; tl < a.nt; tl += nwarps) {
+        const long t = a.t0 + tl;
+        const int ii = inst_of(a.mc, a.n_inst, t);
+        const InstMC& I = a.mc[ii];
+        const float2 x = a.pos[t];
+        const double R = sqrt(double(I.Lx) * I.Lx + double(I.Ly) * I.Ly);   // as the FP64 path
+        const double alpha = 1.0 / (2.0 * kPiD * R);
+        const double mux = double(I.dt) * a.lam_next[2 * t], muy = double(I.dt) * a.lam_next[2 * t + 1];
+        double ltx = 0.0, lty = 0.0;
+        for (int s = 0; s < 2; ++s) {
+            const double sg = (s == 0 ? inv : -inv);
+            const double vx = mux * sg, vy = muy * sg;
+            const double cum = a.cum64[2 * ii + s];
+            const long base = (tl * 2 + s) * Q;
+            double dca = 0.0, csa = 0.0;
+            for (int j = lane; j < Q; j += 32) {
+                const long sid = base + j;
+                const double f = a.fg[3 * sid];
+                double gxx, gxy, df, dc, cv;
+                mis_term_adj(I.law, x, a.ys[sid], f, w1, w2, cum, alpha, R, I, vx, vy, gxx, gxy, df, dc, cv);
+                ltx += gxx;
+                lty += gxy;
+                const double dyx = -gxx + df * a.fg[3 * sid + 1], dyy = -gxy + df * a.fg[3 * sid + 2];
+                if (j >= a.N1) {
+                    ltx += dyx;
+                    lty += dyy;
+                } else {
+                    const int p = a.src[sid];
+                    if (p >= 0 && (dyx != 0.0 || dyy != 0.0)) {
+                        atomicAdd(&a.lam[2 * p], dyx);
+                        atomicAdd(&a.lam[2 * p + 1], dyy);
+                    }
+                    if (a.gsc && p >= 0 && cv != 0.0) {
+                        atomicAdd(&a.gsc[p], cv);
+                        csa += cv;
+                    }
+                }
+                a.as[sid] = df;
+                dca += dc;
+            }
+            dca = warp_sum_d(dca);
+            if (lane == 0 && dca != 0.0) atomicAdd(&a.dcum[2 * ii + s], dca);
+            if (a.gsc) {
+                csa = warp_sum_d(csa);
+                if (lane == 0 && csa != 0.0) atomicAdd(&a.csum[2 * ii + s], csa);
+            }
+        }
+        ltx = warp_sum_d(ltx);
+        lty = warp_sum_d(lty);
+        if (lane == 0) {
+            atomicAdd(&a.lam[2 * t], ltx);
+            atomicAdd(&a.lam[2 * t + 1], lty);
+        }
+    }
+}
+
+// Samples (already grouped by bin in query-record order) as candidates of the
+// transposed sum: weight 2 sigma dc/df (FP32 hi + lo), image flags in pad.
+__global__ void k_adj_dual_cand(const QRec* __restrict__ qrec, const uint32_t* __restrict__ total, long M,
+                                const double* __restrict__ as, const uint32_t* __restrict__ qbin,
+                                const GridInst* __restrict__ inst, int n_inst, Cand* __restrict__ out) {
+    const long n = min(long(*total), M);
+    for (long k = long(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += long(gridDim.x) * blockDim.x) {
+        const QRec r = qrec[k];
+        const uint32_t b = qbin[r.id];
+        int lo = 0, hi = n_inst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (uint32_t(inst[mid].bin_base) <= b) lo = mid; else hi = mid - 1;
+        }
+        const double h = inst[lo].hw;
+        const double w = as[r.id] * (80.0 / (7.0 * kPiD * h * h));
+        const float wh = float(w);
+        out[k] = Cand{r.x, r.x, r.y, r.y, wh, wh, float(w - double(wh)), __uint_as_float(r.flags)};
+    }
+}
+
+// Particles in bin order as queries (self queries of the grid).
+__global__ void k_adj_self(const Cand* __restrict__ cand, const uint32_t* __restrict__ perm,
+                           const uint32_t* __restrict__ start, long n, uint32_t nbins, QRec* __restrict__ q) {
+    const long nv = start[nbins];
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x)
+        q[p] = QRec{cand[p].x, cand[p].y, perm[p], (2u) | (2u << 3)};
+}
+
+__global__ void k_adj_sources(const float* __restrict__ omega, long n, const double* __restrict__ dual,
+                              double* __restrict__ lam, double* __restrict__ gom) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const float w = omega[i];
+        if (w == 0.f) continue;
+        const double aw = fabs(double(w));
+        gom[i] += (w > 0.f ? 1.0 : -1.0) * dual[3 * i];
+        lam[2 * i] += aw * dual[3 * i + 1];
+        lam[2 * i + 1] += aw * dual[3 * i + 2];
+    }
+}
+
+// Omega terms, and (score) the score-function term of the discrete branch-1
+// draw P(I = J) = |omega_J| / Omega_s: d log P(I)/d omega_J =
+// sgn(omega_J) (delta_IJ / |omega_J| - 1 / Omega_s), weighted by each sample's c.
+__global__ void k_adj_cum(const InstMC* __restrict__ mc, int n_inst, const float* __restrict__ omega, long n,
+                          const double* __restrict__ dcum, const double* __restrict__ cum64,
+                          const double* __restrict__ gsc, const double* __restrict__ csum,
+                          double* __restrict__ gom) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const float w = omega[i];
+        if (w == 0.f) continue;
+        const int ii = inst_of(mc, n_inst, i);
+        const int s = w > 0.f ? 0 : 1;
+        const double sg = w > 0.f ? 1.0 : -1.0;
+        const double f9 = mc[ii].periodic ? 9.0 : 1.0;
+        double g = f9 * dcum[2 * ii + s];
+        if (gsc) g += gsc[i] / fabs(double(w)) - csum[2 * ii + s] / (cum64[2 * ii + s] / f9);
+        gom[i] += sg * g;
+    }
+}
+
+// Adjoint working set (allocated on first use): per chunk of samples the
+// source index, FP64 value + gradient, dc/df and the transposed candidates;
+// per particle the self queries, the transposed sums, two lambda buffers and
+// dL/domega.
+struct AdjBufs {
+    int* src;
+    double* fg;
+    double* as;
+    Cand* dual;
+    QRec* selfq;
+    double* dual_out;
+    double* lam[2];
+    double* gom;
+    double* dcum;
+    double* gsc;
+    double* csum;
+};
+
+int adj_bufs(vpmc_sim* s, AdjBufs* A) {
+    const long ns = s->chunk_targets * 2 * samples_per(s);
+    auto carve = [&](Carver& c) {
+        A->src = c.take<int>(size_t(ns));
+        A->fg = c.take<double>(3 * size_t(ns));
+        A->as = c.take<double>(size_t(ns));
+        A->dual = c.take<Cand>(size_t(ns));
+        A->selfq = c.take<QRec>(size_t(s->N));
+        A->dual_out = c.take<double>(3 * size_t(s->N));
+        A->lam[0] = c.take<double>(2 * size_t(s->N));
+        A->lam[1] = c.take<double>(2 * size_t(s->N));
+        A->gom = c.take<double>(size_t(s->N));
+        A->dcum = c.take<double>(2 * size_t(s->n_inst));
+        A->gsc = c.take<double>(size_t(s->N));
+        A->csum = c.take<double>(2 * size_t(s->n_inst));
+    };
+    Carver dry;
+    carve(dry);
+    VPMC_TRY(s->adj.reserve(dry.off));
+    Carver c{static_cast<char*>(s->adj.p), 0};
+    carve(c);
+    return VPMC_OK;
+}
+
+// lam_out = lam_in + (dX'/dX)^T lam_in; gom += (dX'/domega)^T lam_in, at the
+// state in s->pos with the step counter already on the device.
+int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out, bool score) {
+    vpmc_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
+    VPMC_LAUNCH(k_adj_self, blocks_for(s->N), 256, 0, st, s->g.cand, s->g.perm, s->g.start, s->N,
+                uint32_t(s->g.nbins), A.selfq);
+    VPMC_CUDA(cudaMemcpyAsync(lam_out, lam_in, 2 * sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+    VPMC_CUDA(cudaMemsetAsync(A.dcum, 0, 2 * sizeof(double) * size_t(s->n_inst), st));
+    if (score) {
+        VPMC_CUDA(cudaMemsetAsync(A.gsc, 0, sizeof(double) * size_t(s->N), st));
+        VPMC_CUDA(cudaMemsetAsync(A.csum, 0, 2 * sizeof(double) * size_t(s->n_inst), st));
+    }
+    const bool unb = s->mc[0].law == VPMC_LAW_UNBIASED;
+    const long Q = samples_per(s);
+    for (long t0 = 0; t0 < s->N; t0 += s->chunk_targets) {
+        const long nt = std::min(s->chunk_targets, s->N - t0);
+        const long ns = nt * 2 * Q;
+        VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
+        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
+                   nt, s->N1, s->N2, 1, A.src, s->ys, s->q.qbin, s->q.qcount, s->q.qrank};
+        VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
+        VPMC_TRY(scatter_ranked(ctx, s->g, s->q, s->ys, ns));
+        // f and grad f at every sample (FP64)
+        VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(4)));
+        VPMC_CUDA(cudaMemsetAsync(A.fg, 0, 3 * sizeof(double) * size_t(ns), st));
+        EvalLaunch L;
+        L.mode = unb ? EVAL_GRAD9_64 : EVAL_GRAD64;
+        L.qpt = 4;
+        L.out_f64 = A.fg;
+        VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
+        AdjArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, A.fg, A.src, s->cum64, t0, nt, s->N1, s->N2, lam_in, lam_out,
+                   A.as, A.dcum, score ? A.gsc : nullptr, A.csum};
+        VPMC_LAUNCH(k_adj_terms, blocks_for(nt * 32), 256, 0, st, aa);
+        // transposed sum: particles query the chunk's samples
+        VPMC_LAUNCH(k_adj_dual_cand, blocks_for(ns), 256, 0, st, s->q.qrec, s->q.qstart + s->g.nbins, ns, A.as,
+                    s->q.qbin, s->g.inst, s->g.n_inst, A.dual);
+        GridBufs gd = s->g;
+        gd.start = s->q.qstart;
+        gd.cand = A.dual;
+        VPMC_TRY(make_items(ctx, s->g, s->g.start, s->it, query_chunk(4)));
+        VPMC_CUDA(cudaMemsetAsync(A.dual_out, 0, 3 * sizeof(double) * size_t(s->N), st));
+        EvalLaunch D;
+        D.mode = unb ? EVAL_DUAL9_64 : EVAL_DUAL64;
+        D.qpt = 4;
+        D.out_f64 = A.dual_out;
+        VPMC_TRY(launch_eval(ctx, gd, A.selfq, s->it, D));
+        VPMC_LAUNCH(k_adj_sources, blocks_for(s->N), 256, 0, st, s->omega, s->N, A.dual_out, lam_out, A.gom);
+    }
+    VPMC_LAUNCH(k_adj_cum, blocks_for(s->N), 256, 0, st, s->d_mc, s->n_inst, s->omega, s->N, A.dcum, s->cum64,
+                score ? A.gsc : nullptr, A.csum, A.gom);
+    return VPMC_OK;
+}
+
+}  // namespace
+}  // namespace vpmc
+
+using namespace vpmc;
+using namespace vpmc::sim;
+
+extern "C" {
+
+int vpmc_sim_record(vpmc_sim* s, int nsteps, int k_ckpt) {
+    if (!s || nsteps < 1 || k_ckpt < 1) return VPMC_ERR_INVALID;
+    if (s->deform) return VPMC_ERR_UNSUPPORTED;   // the adjoint covers the plain method
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
+    cudaStream_t st = s->ctx->stream;
+    const long nck = (nsteps + k_ckpt - 1) / k_ckpt + 1;   // X_0, X_k, ..., and X_T
+    VPMC_TRY(s->ckpt.reserve(sizeof(float2) * size_t(s->N) * size_t(nck)));
+    float2* ck = static_cast<float2*>(s->ckpt.p);
+    s->rec_steps = nsteps;
+    s->rec_k = k_ckpt;
+    s->rec_step0 = s->step;
+    for (int n = 0; n < nsteps; ++n) {
+        if (n % k_ckpt == 0)
+            VPMC_CUDA(cudaMemcpyAsync(ck + size_t(n / k_ckpt) * s->N, s->pos, sizeof(float2) * size_t(s->N),
+                                      cudaMemcpyDeviceToDevice, st));
+        VPMC_TRY(run_pass(s, true, 1));
+    }
+    VPMC_CUDA(cudaMemcpyAsync(ck + size_t(nck - 1) * s->N, s->pos, sizeof(float2) * size_t(s->N),
+                              cudaMemcpyDeviceToDevice, st));
+    return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_adjoint(vpmc_sim* s, const double* dL_dXT, double* dL_dX0, double* dL_domega, int flags) {
+    if (!s || !dL_dXT || !dL_dX0 || !dL_domega) return VPMC_ERR_INVALID;
+    if (s->rec_steps < 1) return VPMC_ERR_INVALID;   // vpmc_sim_record first
+    if (s->deform) return VPMC_ERR_UNSUPPORTED;
+    vpmc_context* ctx = s->ctx;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    AdjBufs A;
+    VPMC_TRY(adj_bufs(s, &A));
+    const int T = s->rec_steps, k = s->rec_k;
+    const long nck = (T + k - 1) / k + 1;
+    float2* ck = static_cast<float2*>(s->ckpt.p);
+    VPMC_TRY(s->seg.reserve(sizeof(float2) * size_t(s->N) * size_t(k)));
+    float2* seg = static_cast<float2*>(s->seg.p);
+    VPMC_CUDA(cudaMemcpyAsync(A.lam[0], dL_dXT, 2 * sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+    VPMC_CUDA(cudaMemsetAsync(A.gom, 0, sizeof(double) * size_t(s->N), st));
+    int cur = 0;
+    for (long sg = nck - 2; sg >= 0; --sg) {
+        const int n0 = int(sg) * k, n1 = std::min(T, n0 + k);
+        // recompute the segment's states from its checkpoint (bitwise the forward's)
+        VPMC_CUDA(cudaMemcpyAsync(s->pos, ck + size_t(sg) * s->N, sizeof(float2) * size_t(s->N),
+                                  cudaMemcpyDeviceToDevice, st));
+        VPMC_TRY(set_step_counter(s, s->rec_step0 + uint64_t(n0)));
+        for (int n = n0; n < n1; ++n) {
+            VPMC_CUDA(cudaMemcpyAsync(seg + size_t(n - n0) * s->N, s->pos, sizeof(float2) * size_t(s->N),
+                                      cudaMemcpyDeviceToDevice, st));
+            if (n + 1 < n1) VPMC_TRY(run_pass(s, true, 1));
+        }
+        for (int n = n1 - 1; n >= n0; --n) {
+            VPMC_CUDA(cudaMemcpyAsync(s->pos, seg + size_t(n - n0) * s->N, sizeof(float2) * size_t(s->N),
+                                      cudaMemcpyDeviceToDevice, st));
+            VPMC_TRY(set_step_counter(s, s->rec_step0 + uint64_t(n)));
+            VPMC_TRY(adjoint_step(s, A, A.lam[cur], A.lam[cur ^ 1], (flags & VPMC_ADJ_SCORE) != 0));
+            cur ^= 1;
+        }
+    }
+    VPMC_CUDA(cudaMemcpyAsync(dL_dX0, A.lam[cur], 2 * sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+    VPMC_CUDA(cudaMemcpyAsync(dL_domega, A.gom, sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+    // back to the recorded final state
+    VPMC_CUDA(cudaMemcpyAsync(s->pos, ck + size_t(nck - 1) * s->N, sizeof(float2) * size_t(s->N),
+                              cudaMemcpyDeviceToDevice, st));
+    VPMC_TRY(set_step_counter(s, s->rec_step0 + uint64_t(T)));
+    return vpmc_context_sync(ctx);
+}
+
+}  // extern "C"
