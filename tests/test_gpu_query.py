@@ -72,7 +72,7 @@ def test_query_small_domain_counts_each_particle_once(cuda):
     assert _rel(got, want) < 1e-5
 
 
-def test_query_deformed_kernel_unsupported(cuda):
+def test_query_rejects_degenerate_F(cuda):
     import torch
     from vortexparticlemc_cuda_gb300 import phash as P
     from vortexparticlemc_cuda_gb300._lib import VpmcError
