@@ -179,6 +179,26 @@ def test_fp64_path_matches_fp32_path(cuda, law):
     assert np.array_equal(sim.velocity(step=3).cpu().numpy(), v32)
 
 
+def test_positions_after_100_steps_fp32_vs_fp64_common_random_numbers(cuda):
+    """SURVEY-style precision report on the small Taylor-Green case (64^2,
+    N1 = N2 = 16, 100 steps at dt = 1e-3): positions of the FP32-compensated
+    run against the all-FP64 run of the same law with the same samples."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    runs = []
+    for bits in (32, 64):
+        sim, pos, om, prm = _setup(cuda, law=1)
+        sim.set_precision(bits)
+        sim.set_step(0)
+        sim.step(100)
+        runs.append(sim.particles()[0].cpu().numpy().astype(np.float64))
+    d = runs[0] - runs[1]
+    d -= np.round(d)
+    rms = np.sqrt(np.mean(np.sum(d ** 2, 1)))
+    disp = np.sqrt(np.mean(np.sum((runs[1] - pos - np.round(runs[1] - pos)) ** 2, 1)))
+    print(f"position RMS difference FP32 vs FP64 after 100 steps: {rms:.3e} (RMS displacement {disp:.3e})")
+    assert rms < 1e-3 * disp, (rms, disp)
+
+
 def test_empty_sign_subset(cuda):
     """All strengths positive: the negative branch contributes nothing (the
     reference would index sub[-1])."""

@@ -207,15 +207,16 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
     }
 }
 
-// Two-pass placement of ranked samples.  The final slot of sample m is
+// Placement of ranked samples (three streaming passes).  The final slot of sample m is
 // qstart[bin] + qrank[m]; writing 16-byte records straight there touches a
 // different DRAM sector per sample (the bins of consecutive samples are
 // unrelated), so the placement goes through coarse super-bins (2^S
 // consecutive bins): pass 1 moves each CTA's tile of samples into runs per
 // super-bin (one global atomic per CTA and super-bin) as {unwrapped point,
-// sample id, final slot}, pass 2 streams the super-bin segments, wraps each
-// point (deriving its image flags) and writes the record to its final slot
-// -- a region the size of one super-bin at a time, which stays in L2.
+// sample id, final slot}; pass 2 (k_scatter_window) splits the super-bin
+// segments into windows of 2048 final slots; pass 3 (k_scatter_assemble)
+// builds each window in shared memory (wrapping the points and deriving their
+// image flags) and writes it out contiguously.
 constexpr int kCoarseTile = 16;       // samples per thread per tile
 constexpr int kCoarseThreads = 256;   // 4096 samples per tile
 constexpr int kMaxSuper = 2048;
@@ -263,23 +264,117 @@ __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2*
     }
 }
 
-__global__ void k_scatter_fine(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total, long M,
-                               const uint32_t* __restrict__ qbin, const GridInst* __restrict__ inst, int n_inst,
-                               QRec* __restrict__ qrec) {
-    const long n = min(long(*total), M);
-    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
-        const uint4 r = tmp[i];
-        float2 p = make_float2(__uint_as_float(r.x), __uint_as_float(r.y));
-        const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, qbin[r.z])];
-        uint32_t fl = (2u) | (2u << 3);
-        if (G.periodic) {
-            const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
-            p.x = p.x - kx * G.Lx;
-            p.y = p.y - ky * G.Ly;
-            const int ikx = min(max(int(kx), -2), 2), iky = min(max(int(ky), -2), 2);
-            fl = uint32_t(ikx + 2) | (uint32_t(iky + 2) << 3);
+// Query record of a placed sample: wrapped point and image flags (the
+// instance is found from the slot: instances own consecutive bin ranges).
+__device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ inst, int n_inst,
+                                          const uint32_t* __restrict__ qstart) {
+    int ii = 0;
+    if (n_inst > 1) {
+        int lo = 0, hi = n_inst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (qstart[inst[mid].bin_base] <= r.w) lo = mid; else hi = mid - 1;
         }
-        qrec[r.w] = QRec{p.x, p.y, r.z, fl};
+        ii = lo;
+    }
+    const GridInst& G = inst[ii];
+    float2 p = make_float2(__uint_as_float(r.x), __uint_as_float(r.y));
+    uint32_t fl = (2u) | (2u << 3);
+    if (G.periodic) {
+        const float kx = floorf(p.x / G.Lx), ky = floorf(p.y / G.Ly);
+        p.x = p.x - kx * G.Lx;
+        p.y = p.y - ky * G.Ly;
+        const int ikx = min(max(int(kx), -2), 2), iky = min(max(int(ky), -2), 2);
+        fl = uint32_t(ikx + 2) | (uint32_t(iky + 2) << 3);
+    }
+    return QRec{p.x, p.y, r.z, fl};
+}
+
+// Pass 2: the super-bin-grouped records into slot windows of 2^kWinShift
+// slots.  A window's records are exactly the samples whose final slots lie in
+// it, so window w starts at w << kWinShift in the second staging array; each
+// CTA reserves its runs with one atomic per window it touches.  A tile whose
+// slots span more windows than the local histogram holds (a very skewed
+// super-bin) writes its records straight to their final slots instead.
+constexpr int kWinShift = 11;          // 2048 slots = 32 KB of query records per window
+constexpr int kWinTile = 16;           // records per thread per tile
+constexpr int kWinMax = 4096;          // windows one tile may span
+
+__global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total,
+                                                         long M, const GridInst* __restrict__ inst, int n_inst,
+                                                         const uint32_t* __restrict__ qstart,
+                                                         uint32_t* __restrict__ win_fill, uint4* __restrict__ tmp2,
+                                                         QRec* __restrict__ qrec) {
+    __shared__ uint32_t hist[kWinMax];
+    __shared__ uint32_t s_lo, s_hi;
+    const long n = min(long(*total), M);
+    const long tile = long(kWinTile) * blockDim.x;
+    for (long t0 = long(blockIdx.x) * tile; t0 < n; t0 += long(gridDim.x) * tile) {
+        if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
+        __syncthreads();
+        uint4 r[kWinTile];
+        uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int j = 0; j < kWinTile; ++j) {
+            const long i = t0 + long(j) * blockDim.x + threadIdx.x;
+            r[j] = i < n ? tmp[i] : make_uint4(0u, 0u, 0u, 0xffffffffu);
+            if (i < n) { lo = min(lo, r[j].w >> kWinShift); hi = max(hi, r[j].w >> kWinShift); }
+        }
+        atomicMin(&s_lo, lo);
+        atomicMax(&s_hi, hi);
+        __syncthreads();
+        const uint32_t wlo = s_lo, span = s_hi >= s_lo ? s_hi - s_lo + 1u : 0u;
+        if (span > uint32_t(kWinMax)) {
+#pragma unroll
+            for (int j = 0; j < kWinTile; ++j)
+                if (r[j].w != 0xffffffffu) qrec[r[j].w] = make_qrec(r[j], inst, n_inst, qstart);
+            __syncthreads();
+            continue;
+        }
+        for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) hist[k] = 0u;
+        __syncthreads();
+        uint32_t lr[kWinTile];
+#pragma unroll
+        for (int j = 0; j < kWinTile; ++j)
+            if (r[j].w != 0xffffffffu) lr[j] = atomicAdd(&hist[(r[j].w >> kWinShift) - wlo], 1u);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) {
+            const uint32_t c = hist[k];
+            if (c) hist[k] = ((wlo + k) << kWinShift) + atomicAdd(&win_fill[wlo + k], c);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kWinTile; ++j)
+            if (r[j].w != 0xffffffffu) tmp2[hist[(r[j].w >> kWinShift) - wlo] + lr[j]] = r[j];
+        __syncthreads();
+    }
+}
+
+// Pass 3: one window per CTA: its records are assembled in shared memory in
+// slot order and written out as one contiguous block.
+__global__ void __launch_bounds__(256) k_scatter_assemble(const uint4* __restrict__ tmp2,
+                                                           const uint32_t* __restrict__ win_fill,
+                                                           const uint32_t* __restrict__ total, long M,
+                                                           const GridInst* __restrict__ inst, int n_inst,
+                                                           const uint32_t* __restrict__ qstart,
+                                                           QRec* __restrict__ qrec) {
+    __shared__ QRec buf[1 << kWinShift];
+    const long n = min(long(*total), M);
+    const long nwin = (n + (1L << kWinShift) - 1) >> kWinShift;
+    for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
+        const long base = w << kWinShift;
+        const int cnt = int(min(1L << kWinShift, n - base));
+        const int have = int(win_fill[w]);   // < cnt only where a skewed tile wrote its records directly
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) buf[k].id = 0xffffffffu;
+        __syncthreads();
+        for (int k = threadIdx.x; k < have; k += blockDim.x) {
+            const uint4 r = tmp2[base + k];
+            buf[r.w - uint32_t(base)] = make_qrec(r, inst, n_inst, qstart);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+            if (buf[k].id != 0xffffffffu) qrec[base + k] = buf[k];
+        __syncthreads();
     }
 }
 
@@ -1054,7 +1149,9 @@ void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool tw
     q->qrank = c.take<uint32_t>(m);
     q->qrec = c.take<QRec>(m);
     q->tmp = two_pass ? c.take<uint4>(m) : nullptr;
+    q->tmp2 = two_pass ? c.take<uint4>(m) : nullptr;
     q->super_fill = two_pass ? c.take<uint32_t>(kMaxSuper + 1) : nullptr;
+    q->win_fill = two_pass ? c.take<uint32_t>((m >> kWinShift) + 2) : nullptr;
     q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
 }
 
@@ -1080,8 +1177,13 @@ int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
         const int grid = int(std::min<long>(tiles, 8L * ctx->sm_count));
         VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), kCoarseThreads, 0, st, pts, M, q.qbin, q.qrank, q.qstart,
                     shift, nsuper, q.super_fill, q.tmp);
-        VPMC_LAUNCH(k_scatter_fine, blocks_for(M), 256, 0, st, q.tmp, q.qstart + g.nbins, M, q.qbin, g.inst,
-                    g.n_inst, q.qrec);
+        const long nwin = (M >> kWinShift) + 2;
+        VPMC_CUDA(cudaMemsetAsync(q.win_fill, 0, sizeof(uint32_t) * size_t(nwin), st));
+        const long wtiles = (M + long(kWinTile) * 256 - 1) / (long(kWinTile) * 256);
+        VPMC_LAUNCH(k_scatter_window, int(std::max<long>(1, std::min<long>(wtiles, 8L * ctx->sm_count))), 256, 0, st,
+                    q.tmp, q.qstart + g.nbins, M, g.inst, g.n_inst, q.qstart, q.win_fill, q.tmp2, q.qrec);
+        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, 32L * ctx->sm_count))), 256, 0, st,
+                    q.tmp2, q.win_fill, q.qstart + g.nbins, M, g.inst, g.n_inst, q.qstart, q.qrec);
         return VPMC_OK;
     }
     VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, ctx->stream, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,

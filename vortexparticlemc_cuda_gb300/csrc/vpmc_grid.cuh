@@ -166,8 +166,10 @@ struct QueryBufs {
     uint32_t* qfill = nullptr;   // nbins
     uint32_t* qrank = nullptr;   // per point: rank inside its bin (from the counting atomic)
     QRec* qrec = nullptr;        // max points
-    uint4* tmp = nullptr;        // max points (two-pass placement of ranked points)
+    uint4* tmp = nullptr;        // max points (staged placement of ranked points: super-bins)
+    uint4* tmp2 = nullptr;       // max points (staged placement: slot windows)
     uint32_t* super_fill = nullptr;
+    uint32_t* win_fill = nullptr;
     uint32_t* scan_tmp = nullptr;
 };
 void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool two_pass = false);
@@ -179,7 +181,8 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M,
                    int field9);
 // Same, with each point's rank inside its bin already in q.qrank (no atomics;
-// through super-bins in two streaming passes when q.tmp is carved).
+// through super-bins and slot windows in three streaming passes when q.tmp
+// is carved).
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M);
 
 // sigma_max over F[0..n) (+inf if some F is non-finite or has det <= 0);
