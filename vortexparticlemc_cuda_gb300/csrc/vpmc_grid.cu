@@ -220,7 +220,7 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 constexpr int kCoarseTile = 16;       // samples per thread per tile
 constexpr int kCoarseThreads = 256;   // 4096 samples per tile
 constexpr int kMaxSuper = 2048;
-constexpr int kTargetSuper = 1024;    // super-bins per grid: one super-bin region at a time stays in L2
+constexpr int kTargetSuper = 256;     // super-bins per grid (runs of ~16 records per tile and super-bin)
 
 __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
                                                          const uint32_t* __restrict__ qbin,
@@ -298,7 +298,7 @@ __device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ 
 // super-bin) writes its records straight to their final slots instead.
 constexpr int kWinShift = 11;          // 2048 slots = 32 KB of query records per window
 constexpr int kWinTile = 16;           // records per thread per tile
-constexpr int kWinMax = 4096;          // windows one tile may span
+constexpr int kWinMax = 8192;          // windows one tile may span (32 KB of counters)
 
 __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total,
                                                          long M, const GridInst* __restrict__ inst, int n_inst,
