@@ -289,7 +289,7 @@ def run_gpu(args, wl):
         # the reference's step_cuda: deformed kernels, 5-point auxiliary targets, F update
         sim.set_deformation(True)
     if args.precision == 64:
-        # the plain FP64 GPU path of the same estimator (the spec comparison baseline)
+        # the plain FP64 GPU path of the same estimator (the comparison baseline of the FP32 path)
         sim.set_precision(64)
 
     # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
@@ -381,7 +381,7 @@ def run_gpu(args, wl):
                                        " (field evaluation at MIS samples)",
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
             "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
-                           f"({peak_kind}); no tensor-core or HBM bound applies (H3)",
+                           f"({peak_kind}); the kernel is FP32-pipe bound: no tensor-core or HBM bound applies",
             "traffic": None if args.deform else profile_traffic(args.workload),
             "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.0f} in-support pairs x 16 flop",
             "eval_ms_per_launch": eval_ms_launch, "eval_share_of_step": float(np.mean(eval_ms)) / (ms / args.steps)}

@@ -365,9 +365,8 @@ uint64_t vpmc_sim_get_step(vpmc_sim* sim);
 /* Arithmetic of the MIS step: 32 (default: FP32 pair arithmetic with
  * compensated sums) or 64 (the plain FP64 path of the same estimator: field
  * values, MIS terms, sums and the Euler update in FP64; sample points are
- * drawn as in FP32 mode).  The FP64 path exists as the comparison baseline
- * north of which the FP32 path is measured; on GB300 FP64 runs at a small
- * fraction of the FP32 rate. */
+ * drawn as in FP32 mode).  The FP64 path is the baseline the FP32 path is
+ * measured against; on GB300 FP64 runs at a small fraction of the FP32 rate. */
 int vpmc_sim_set_precision(vpmc_sim* sim, int bits);
 
 /* Neighbour-walk tuning: cells per h_w (1 <= k <= 8; the walk covers the

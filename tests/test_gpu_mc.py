@@ -180,7 +180,7 @@ def test_fp64_path_matches_fp32_path(cuda, law):
 
 
 def test_positions_after_100_steps_fp32_vs_fp64_common_random_numbers(cuda):
-    """SURVEY-style precision report on the small Taylor-Green case (64^2,
+    """Precision report on the small Taylor-Green case (64^2,
     N1 = N2 = 16, 100 steps at dt = 1e-3): positions of the FP32-compensated
     run against the all-FP64 run of the same law with the same samples."""
     from vortexparticlemc_cuda_gb300 import phash as P
