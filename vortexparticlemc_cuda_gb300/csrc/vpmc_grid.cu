@@ -207,16 +207,21 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
     }
 }
 
-// Placement of ranked samples (three streaming passes).  The final slot of sample m is
-// qstart[bin] + qrank[m]; writing 16-byte records straight there touches a
-// different DRAM sector per sample (the bins of consecutive samples are
-// unrelated), so the placement goes through coarse super-bins (2^S
-// consecutive bins): pass 1 moves each CTA's tile of samples into runs per
-// super-bin (one global atomic per CTA and super-bin) as {unwrapped point,
-// sample id, final slot}; pass 2 (k_scatter_window) splits the super-bin
-// segments into windows of 2048 final slots; pass 3 (k_scatter_assemble)
-// builds each window in shared memory (wrapping the points and deriving their
-// image flags) and writes it out contiguously.
+// Placement of binned samples (three streaming passes).  Writing a 16-byte
+// record straight to its final slot touches a different DRAM sector per
+// sample (the bins of consecutive samples are unrelated).  Instead:
+//   pass 1 (k_scatter_coarse): each CTA moves its tile of samples into runs
+//     per super-bin (2^S consecutive bins; one global atomic per CTA and
+//     super-bin) as {unwrapped point, sample id, bin};
+//   pass 2 (k_scatter_window): the super-bin segments into runs per window
+//     (2^W consecutive bins, ~1-2k samples), placed at the window's first
+//     slot qstart[w << W];
+//   pass 3 (k_scatter_assemble): one CTA per window gives every record its
+//     slot from shared-memory counters started at qstart of its bin, builds
+//     the window in shared memory (wrapping the point, deriving its image
+//     flags) and writes it out as one contiguous block.
+// The order of queries inside a bin is not fixed by this; no result depends
+// on it (each query's field value is its own fixed-order sum).
 constexpr int kCoarseTile = 16;       // samples per thread per tile
 constexpr int kCoarseThreads = 256;   // 4096 samples per tile
 constexpr int kMaxSuper = 2048;
@@ -224,7 +229,6 @@ constexpr int kTargetSuper = 256;     // super-bins per grid (runs of ~16 record
 
 __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
                                                          const uint32_t* __restrict__ qbin,
-                                                         const uint32_t* __restrict__ qrank,
                                                          const uint32_t* __restrict__ qstart, int shift, int nsuper,
                                                          uint32_t* __restrict__ super_fill, uint4* __restrict__ tmp) {
     __shared__ uint32_t hist[kMaxSuper];
@@ -232,18 +236,12 @@ __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2*
     for (long t0 = long(blockIdx.x) * tile; t0 < M; t0 += long(gridDim.x) * tile) {
         for (int k = threadIdx.x; k < nsuper; k += blockDim.x) hist[k] = 0u;
         __syncthreads();
-        uint32_t sb[kCoarseTile], lr[kCoarseTile];
+        uint32_t bb[kCoarseTile], lr[kCoarseTile];
 #pragma unroll
         for (int j = 0; j < kCoarseTile; ++j) {
             const long m = t0 + long(j) * blockDim.x + threadIdx.x;
-            sb[j] = kNoBin;
-            if (m < M) {
-                const uint32_t b = qbin[m];
-                if (b != kNoBin) {
-                    sb[j] = b >> shift;
-                    lr[j] = atomicAdd(&hist[sb[j]], 1u);
-                }
-            }
+            bb[j] = m < M ? qbin[m] : kNoBin;
+            if (bb[j] != kNoBin) lr[j] = atomicAdd(&hist[bb[j] >> shift], 1u);
         }
         __syncthreads();
         for (int k = threadIdx.x; k < nsuper; k += blockDim.x) {
@@ -253,31 +251,19 @@ __global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2*
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kCoarseTile; ++j) {
-            if (sb[j] == kNoBin) continue;
+            if (bb[j] == kNoBin) continue;
             const long m = t0 + long(j) * blockDim.x + threadIdx.x;
-            const uint32_t b = qbin[m];
-            const float2 p = pts[m];   // unwrapped: pass 2 wraps it and derives the image flags
-            tmp[hist[sb[j]] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), uint32_t(m),
-                                                  qstart[b] + qrank[m]);
+            const float2 p = pts[m];   // unwrapped: pass 3 wraps it and derives the image flags
+            tmp[hist[bb[j] >> shift] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), uint32_t(m),
+                                                           bb[j]);
         }
         __syncthreads();
     }
 }
 
-// Query record of a placed sample: wrapped point and image flags (the
-// instance is found from the slot: instances own consecutive bin ranges).
-__device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ inst, int n_inst,
-                                          const uint32_t* __restrict__ qstart) {
-    int ii = 0;
-    if (n_inst > 1) {
-        int lo = 0, hi = n_inst - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (qstart[inst[mid].bin_base] <= r.w) lo = mid; else hi = mid - 1;
-        }
-        ii = lo;
-    }
-    const GridInst& G = inst[ii];
+// Query record of a placed sample: wrapped point and image flags.
+__device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ inst, int n_inst) {
+    const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, r.w)];
     float2 p = make_float2(__uint_as_float(r.x), __uint_as_float(r.y));
     uint32_t fl = (2u) | (2u << 3);
     if (G.periodic) {
@@ -290,21 +276,14 @@ __device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ 
     return QRec{p.x, p.y, r.z, fl};
 }
 
-// Pass 2: the super-bin-grouped records into slot windows of 2^kWinShift
-// slots.  A window's records are exactly the samples whose final slots lie in
-// it, so window w starts at w << kWinShift in the second staging array; each
-// CTA reserves its runs with one atomic per window it touches.  A tile whose
-// slots span more windows than the local histogram holds (a very skewed
-// super-bin) writes its records straight to their final slots instead.
-constexpr int kWinShift = 11;          // 2048 slots = 32 KB of query records per window
 constexpr int kWinTile = 16;           // records per thread per tile
-constexpr int kWinMax = 8192;          // windows one tile may span (32 KB of counters)
+constexpr int kWinMax = 8192;          // windows one tile may count in shared memory
+constexpr int kWinCap = 4096;          // records a window assembles in shared memory (64 KB)
+constexpr int kWinBinsMax = 1024;      // bins per window at most (shared-memory counters)
 
 __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total,
-                                                         long M, const GridInst* __restrict__ inst, int n_inst,
-                                                         const uint32_t* __restrict__ qstart,
-                                                         uint32_t* __restrict__ win_fill, uint4* __restrict__ tmp2,
-                                                         QRec* __restrict__ qrec) {
+                                                         long M, int wshift, const uint32_t* __restrict__ qstart,
+                                                         uint32_t* __restrict__ win_fill, uint4* __restrict__ tmp2) {
     __shared__ uint32_t hist[kWinMax];
     __shared__ uint32_t s_lo, s_hi;
     const long n = min(long(*total), M);
@@ -317,17 +296,21 @@ __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict_
 #pragma unroll
         for (int j = 0; j < kWinTile; ++j) {
             const long i = t0 + long(j) * blockDim.x + threadIdx.x;
-            r[j] = i < n ? tmp[i] : make_uint4(0u, 0u, 0u, 0xffffffffu);
-            if (i < n) { lo = min(lo, r[j].w >> kWinShift); hi = max(hi, r[j].w >> kWinShift); }
+            r[j] = i < n ? tmp[i] : make_uint4(0u, 0u, 0u, kNoBin);
+            if (r[j].w != kNoBin) { lo = min(lo, r[j].w >> wshift); hi = max(hi, r[j].w >> wshift); }
         }
         atomicMin(&s_lo, lo);
         atomicMax(&s_hi, hi);
         __syncthreads();
         const uint32_t wlo = s_lo, span = s_hi >= s_lo ? s_hi - s_lo + 1u : 0u;
         if (span > uint32_t(kWinMax)) {
+            // a tile across many sparse super-bins: one global atomic per record
 #pragma unroll
-            for (int j = 0; j < kWinTile; ++j)
-                if (r[j].w != 0xffffffffu) qrec[r[j].w] = make_qrec(r[j], inst, n_inst, qstart);
+            for (int j = 0; j < kWinTile; ++j) {
+                if (r[j].w == kNoBin) continue;
+                const uint32_t w = r[j].w >> wshift;
+                tmp2[qstart[w << wshift] + atomicAdd(&win_fill[w], 1u)] = r[j];
+            }
             __syncthreads();
             continue;
         }
@@ -336,44 +319,43 @@ __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict_
         uint32_t lr[kWinTile];
 #pragma unroll
         for (int j = 0; j < kWinTile; ++j)
-            if (r[j].w != 0xffffffffu) lr[j] = atomicAdd(&hist[(r[j].w >> kWinShift) - wlo], 1u);
+            if (r[j].w != kNoBin) lr[j] = atomicAdd(&hist[(r[j].w >> wshift) - wlo], 1u);
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) {
             const uint32_t c = hist[k];
-            if (c) hist[k] = ((wlo + k) << kWinShift) + atomicAdd(&win_fill[wlo + k], c);
+            if (c) hist[k] = qstart[(wlo + k) << wshift] + atomicAdd(&win_fill[wlo + k], c);
         }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kWinTile; ++j)
-            if (r[j].w != 0xffffffffu) tmp2[hist[(r[j].w >> kWinShift) - wlo] + lr[j]] = r[j];
+            if (r[j].w != kNoBin) tmp2[hist[(r[j].w >> wshift) - wlo] + lr[j]] = r[j];
         __syncthreads();
     }
 }
 
-// Pass 3: one window per CTA: its records are assembled in shared memory in
-// slot order and written out as one contiguous block.
-__global__ void __launch_bounds__(256) k_scatter_assemble(const uint4* __restrict__ tmp2,
-                                                           const uint32_t* __restrict__ win_fill,
-                                                           const uint32_t* __restrict__ total, long M,
-                                                           const GridInst* __restrict__ inst, int n_inst,
+__global__ void __launch_bounds__(256) k_scatter_assemble(const uint4* __restrict__ tmp2, long nbins, int wshift,
                                                            const uint32_t* __restrict__ qstart,
+                                                           const GridInst* __restrict__ inst, int n_inst,
                                                            QRec* __restrict__ qrec) {
-    __shared__ QRec buf[1 << kWinShift];
-    const long n = min(long(*total), M);
-    const long nwin = (n + (1L << kWinShift) - 1) >> kWinShift;
+    extern __shared__ __align__(16) QRec buf[];   // kWinCap records
+    __shared__ uint32_t cnt[kWinBinsMax];
+    const long nwin = ((nbins - 1) >> wshift) + 1;
     for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
-        const long base = w << kWinShift;
-        const int cnt = int(min(1L << kWinShift, n - base));
-        const int have = int(win_fill[w]);   // < cnt only where a skewed tile wrote its records directly
-        for (int k = threadIdx.x; k < cnt; k += blockDim.x) buf[k].id = 0xffffffffu;
+        const long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
+        const uint32_t start = qstart[b0], nw = qstart[b1] - start;
+        for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) cnt[b - b0] = qstart[b];
         __syncthreads();
-        for (int k = threadIdx.x; k < have; k += blockDim.x) {
-            const uint4 r = tmp2[base + k];
-            buf[r.w - uint32_t(base)] = make_qrec(r, inst, n_inst, qstart);
+        const bool fits = nw <= uint32_t(kWinCap);
+        for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) {
+            const uint4 r = tmp2[start + k];
+            const uint32_t slot = atomicAdd(&cnt[r.w - uint32_t(b0)], 1u);
+            const QRec q = make_qrec(r, inst, n_inst);
+            if (fits) buf[slot - start] = q;
+            else qrec[slot] = q;   // an over-full window: direct stores
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < cnt; k += blockDim.x)
-            if (buf[k].id != 0xffffffffu) qrec[base + k] = buf[k];
+        if (fits)
+            for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) qrec[start + k] = buf[k];
         __syncthreads();
     }
 }
@@ -1146,12 +1128,12 @@ void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool tw
     q->qcount = c.take<uint32_t>(size_t(nbins + 1));
     q->qstart = c.take<uint32_t>(size_t(nbins + 1));
     q->qfill = c.take<uint32_t>(size_t(nbins + 1));
-    q->qrank = c.take<uint32_t>(m);
+    q->qrank = two_pass ? nullptr : c.take<uint32_t>(m);   // ranks are only needed without the staged placement
     q->qrec = c.take<QRec>(m);
     q->tmp = two_pass ? c.take<uint4>(m) : nullptr;
     q->tmp2 = two_pass ? c.take<uint4>(m) : nullptr;
     q->super_fill = two_pass ? c.take<uint32_t>(kMaxSuper + 1) : nullptr;
-    q->win_fill = two_pass ? c.take<uint32_t>((m >> kWinShift) + 2) : nullptr;
+    q->win_fill = two_pass ? c.take<uint32_t>(size_t(nbins + 1)) : nullptr;
     q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
 }
 
@@ -1167,27 +1149,36 @@ int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
 
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M) {
     VPMC_TRY(exclusive_scan(ctx, q.qcount, q.qstart, g.nbins, q.scan_tmp, true));
-    if (q.tmp && M < (1L << 32)) {
+    cudaStream_t st = ctx->stream;
+    if (q.tmp) {
         int shift = 0;
         while (((g.nbins - 1) >> shift) + 1 > kTargetSuper) ++shift;
         const int nsuper = int(((g.nbins - 1) >> shift) + 1);
-        cudaStream_t st = ctx->stream;
+        // windows of 2^W bins holding ~1024 samples on average
+        const double per_bin = double(M) / double(std::max<long>(g.nbins, 1));
+        int wshift = 0;
+        while (wshift < 10 && per_bin * double(2L << wshift) <= 1024.0) ++wshift;
+        const long nwin = ((g.nbins - 1) >> wshift) + 1;
         VPMC_CUDA(cudaMemsetAsync(q.super_fill, 0, sizeof(uint32_t) * size_t(nsuper), st));
-        const long tiles = (M + long(kCoarseTile) * kCoarseThreads - 1) / (long(kCoarseTile) * kCoarseThreads);
-        const int grid = int(std::min<long>(tiles, 8L * ctx->sm_count));
-        VPMC_LAUNCH(k_scatter_coarse, std::max(grid, 1), kCoarseThreads, 0, st, pts, M, q.qbin, q.qrank, q.qstart,
-                    shift, nsuper, q.super_fill, q.tmp);
-        const long nwin = (M >> kWinShift) + 2;
         VPMC_CUDA(cudaMemsetAsync(q.win_fill, 0, sizeof(uint32_t) * size_t(nwin), st));
+        const long tiles = (M + long(kCoarseTile) * kCoarseThreads - 1) / (long(kCoarseTile) * kCoarseThreads);
+        VPMC_LAUNCH(k_scatter_coarse, int(std::max<long>(1, std::min<long>(tiles, 8L * ctx->sm_count))),
+                    kCoarseThreads, 0, st, pts, M, q.qbin, q.qstart, shift, nsuper, q.super_fill, q.tmp);
         const long wtiles = (M + long(kWinTile) * 256 - 1) / (long(kWinTile) * 256);
         VPMC_LAUNCH(k_scatter_window, int(std::max<long>(1, std::min<long>(wtiles, 8L * ctx->sm_count))), 256, 0, st,
-                    q.tmp, q.qstart + g.nbins, M, g.inst, g.n_inst, q.qstart, q.win_fill, q.tmp2, q.qrec);
-        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, 32L * ctx->sm_count))), 256, 0, st,
-                    q.tmp2, q.win_fill, q.qstart + g.nbins, M, g.inst, g.n_inst, q.qstart, q.qrec);
+                    q.tmp, q.qstart + g.nbins, M, wshift, q.qstart, q.win_fill, q.tmp2);
+        static bool configured[64] = {};
+        const size_t smem = sizeof(QRec) * size_t(kWinCap);
+        if (ctx->device < 64 && !configured[ctx->device]) {
+            VPMC_CUDA(cudaFuncSetAttribute(k_scatter_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            configured[ctx->device] = true;
+        }
+        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, 16L * ctx->sm_count))), 256, smem,
+                    st, q.tmp2, g.nbins, wshift, q.qstart, g.inst, g.n_inst, q.qrec);
         return VPMC_OK;
     }
-    VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, ctx->stream, pts, M, g.inst, g.n_inst, q.qbin, q.qrank,
-                q.qstart, q.qrec);
+    VPMC_LAUNCH(k_scatter_ranked, blocks_for(M), 256, 0, st, pts, M, g.inst, g.n_inst, q.qbin, q.qrank, q.qstart,
+                q.qrec);
     return VPMC_OK;
 }
 

@@ -164,7 +164,7 @@ struct QueryBufs {
     uint32_t* qcount = nullptr;  // nbins + 1
     uint32_t* qstart = nullptr;  // nbins + 1
     uint32_t* qfill = nullptr;   // nbins
-    uint32_t* qrank = nullptr;   // per point: rank inside its bin (from the counting atomic)
+    uint32_t* qrank = nullptr;   // per point: rank inside its bin (only without the staged placement)
     QRec* qrec = nullptr;        // max points
     uint4* tmp = nullptr;        // max points (staged placement of ranked points: super-bins)
     uint4* tmp2 = nullptr;       // max points (staged placement: slot windows)
@@ -180,9 +180,10 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 // Scatter points whose bins are already in q.qbin (counts in q.qcount).
 int scatter_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M,
                    int field9);
-// Same, with each point's rank inside its bin already in q.qrank (no atomics;
-// through super-bins and slot windows in three streaming passes when q.tmp
-// is carved).
+// Same for points whose bins are counted in q.qcount: with q.tmp carved
+// through super-bins and bin windows in three streaming passes (slots inside
+// a bin assigned in shared memory); otherwise each point's rank inside its
+// bin must be in q.qrank.
 int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2* pts, long M);
 
 // sigma_max over F[0..n) (+inf if some F is non-finite or has det <= 0);

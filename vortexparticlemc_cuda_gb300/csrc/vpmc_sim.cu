@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                 const int cx = min(max(floor_int(px * G.inv_sx), 0), G.gx - 1);
                 const int cy = min(max(floor_int(py * G.inv_sy), 0), G.gy - 1);
                 b = uint32_t(G.bin_base) + uint32_t(s) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
-                // the counting atomic also hands out this sample's slot in its bin
-                a.qrank[sid] = atomicAdd(&a.qcount[b], 1u);
+                if (a.qrank) a.qrank[sid] = atomicAdd(&a.qcount[b], 1u);   // rank in its bin
+                else atomicAdd(&a.qcount[b], 1u);                            // count only
             }
         }
         a.ys[sid] = y;
@@ -747,7 +747,8 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
         GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, def ? s->F : nullptr, s->sub, s->cdf, s->guide, s->jit,
-                   s->d_step, t0, nt, s->N1, s->N2, def ? 5 : 1, nullptr, s->ys, s->q.qbin, s->q.qcount, s->q.qrank};
+                   s->d_step, t0, nt, s->N1, s->N2, def ? 5 : 1, nullptr, s->ys, s->q.qbin, s->q.qcount,
+                   s->q.tmp ? nullptr : s->q.qrank};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
         VPMC_TRY(scatter_ranked(ctx, s->g, s->q, s->ys, ns));
         VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(s->precision == 64 ? 4 : s->qpt)));
