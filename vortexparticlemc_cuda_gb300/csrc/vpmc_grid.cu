@@ -222,40 +222,92 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 //     flags) and writes it out as one contiguous block.
 // The order of queries inside a bin is not fixed by this; no result depends
 // on it (each query's field value is its own fixed-order sum).
-constexpr int kCoarseTile = 16;       // samples per thread per tile
-constexpr int kCoarseThreads = 256;   // 4096 samples per tile
-constexpr int kMaxSuper = 2048;
-constexpr int kTargetSuper = 256;     // super-bins per grid (runs of ~16 records per tile and super-bin)
+constexpr int kPlaceThreads = 256;
+constexpr int kPlaceTile = 16;                               // records per thread per tile
+constexpr int kTileRecs = kPlaceThreads * kPlaceTile;        // 4096 records = 64 KB staged per tile
+constexpr int kTargetSuper = 256;                            // super-bins per grid
+constexpr int kWinMax = 2048;                                // windows one tile may sort in shared memory
+constexpr int kWinCap = 8192;                                // records a window assembles in shared memory
+constexpr int kWinBinsMax = 256;                             // bins per window at most
 
-__global__ void __launch_bounds__(kCoarseThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
-                                                         const uint32_t* __restrict__ qbin,
-                                                         const uint32_t* __restrict__ qstart, int shift, int nsuper,
-                                                         uint32_t* __restrict__ super_fill, uint4* __restrict__ tmp) {
-    __shared__ uint32_t hist[kMaxSuper];
-    const long tile = long(kCoarseTile) * blockDim.x;
-    for (long t0 = long(blockIdx.x) * tile; t0 < M; t0 += long(gridDim.x) * tile) {
-        for (int k = threadIdx.x; k < nsuper; k += blockDim.x) hist[k] = 0u;
-        __syncthreads();
-        uint32_t bb[kCoarseTile], lr[kCoarseTile];
+// Exclusive prefix sum of v[0..n) in place (shared memory, n small), block
+// of kPlaceThreads; returns the total.
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t* v, int n, uint32_t* s_warp) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int per = (n + kPlaceThreads - 1) / kPlaceThreads;
+    const int b = min(n, tid * per), e = min(n, b + per);
+    uint32_t sum = 0;
+    for (int i = b; i < e; ++i) sum += v[i];
+    uint32_t x = sum;
 #pragma unroll
-        for (int j = 0; j < kCoarseTile; ++j) {
-            const long m = t0 + long(j) * blockDim.x + threadIdx.x;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t t = lane < kPlaceThreads / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < kPlaceThreads / 32) s_warp[lane] = t;
+    }
+    __syncthreads();
+    uint32_t run = (x - sum) + (wid > 0 ? s_warp[wid - 1] : 0u);
+    for (int i = b; i < e; ++i) {
+        const uint32_t c = v[i];
+        v[i] = run;
+        run += c;
+    }
+    const uint32_t total = s_warp[kPlaceThreads / 32 - 1];
+    __syncthreads();
+    return total;
+}
+
+// Pass 1: each tile of samples counting-sorted by super-bin in shared memory,
+// one global reservation per (tile, super-bin), then written out as
+// contiguous runs (coalesced stores).
+__global__ void __launch_bounds__(kPlaceThreads) k_scatter_coarse(const float2* __restrict__ pts, long M,
+                                                                 const uint32_t* __restrict__ qbin,
+                                                                 const uint32_t* __restrict__ qstart, int shift,
+                                                                 int nsuper, uint32_t* __restrict__ super_fill,
+                                                                 uint4* __restrict__ tmp) {
+    extern __shared__ __align__(16) uint4 srec[];   // kTileRecs
+    __shared__ uint32_t hist[kTargetSuper], loff[kTargetSuper], s_warp[32];
+    __shared__ long long goff[kTargetSuper];
+    for (long t0 = long(blockIdx.x) * kTileRecs; t0 < M; t0 += long(gridDim.x) * kTileRecs) {
+        for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) hist[k] = 0u;
+        __syncthreads();
+        uint32_t bb[kPlaceTile], lr[kPlaceTile];
+#pragma unroll
+        for (int j = 0; j < kPlaceTile; ++j) {
+            const long m = t0 + long(j) * kPlaceThreads + threadIdx.x;
             bb[j] = m < M ? qbin[m] : kNoBin;
             if (bb[j] != kNoBin) lr[j] = atomicAdd(&hist[bb[j] >> shift], 1u);
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < nsuper; k += blockDim.x) {
+        for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) loff[k] = hist[k];
+        __syncthreads();
+        const uint32_t ntile = block_scan_excl(loff, nsuper, s_warp);
+        for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) {
             const uint32_t c = hist[k];
-            if (c) hist[k] = qstart[uint32_t(k) << shift] + atomicAdd(&super_fill[k], c);
+            goff[k] = c ? (long long)(qstart[uint32_t(k) << shift] + atomicAdd(&super_fill[k], c)) - loff[k] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < kPlaceTile; ++j) {
+            if (bb[j] == kNoBin) continue;
+            const long m = t0 + long(j) * kPlaceThreads + threadIdx.x;
+            const float2 p = pts[m];   // unwrapped: pass 3 wraps it and derives the image flags
+            srec[loff[bb[j] >> shift] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y),
+                                                            uint32_t(m), bb[j]);
         }
         __syncthreads();
-#pragma unroll
-        for (int j = 0; j < kCoarseTile; ++j) {
-            if (bb[j] == kNoBin) continue;
-            const long m = t0 + long(j) * blockDim.x + threadIdx.x;
-            const float2 p = pts[m];   // unwrapped: pass 3 wraps it and derives the image flags
-            tmp[hist[bb[j] >> shift] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), uint32_t(m),
-                                                           bb[j]);
+        for (uint32_t i = threadIdx.x; i < ntile; i += kPlaceThreads) {
+            const uint4 r = srec[i];
+            tmp[goff[r.w >> shift] + i] = r;
         }
         __syncthreads();
     }
@@ -276,26 +328,28 @@ __device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ 
     return QRec{p.x, p.y, r.z, fl};
 }
 
-constexpr int kWinTile = 16;           // records per thread per tile
-constexpr int kWinMax = 8192;          // windows one tile may count in shared memory
-constexpr int kWinCap = 4096;          // records a window assembles in shared memory (64 KB)
-constexpr int kWinBinsMax = 1024;      // bins per window at most (shared-memory counters)
-
-__global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict__ tmp, const uint32_t* __restrict__ total,
-                                                         long M, int wshift, const uint32_t* __restrict__ qstart,
-                                                         uint32_t* __restrict__ win_fill, uint4* __restrict__ tmp2) {
-    __shared__ uint32_t hist[kWinMax];
+// Pass 2: the same per tile of the super-bin-grouped records, by window
+// (2^W consecutive bins), placed from the window's first slot qstart[w << W].
+// A tile spanning more windows than the shared-memory counters hold (one
+// across many sparse super-bins) reserves per record instead.
+__global__ void __launch_bounds__(kPlaceThreads) k_scatter_window(const uint4* __restrict__ tmp,
+                                                                 const uint32_t* __restrict__ total, long M,
+                                                                 int wshift, const uint32_t* __restrict__ qstart,
+                                                                 uint32_t* __restrict__ win_fill,
+                                                                 uint4* __restrict__ tmp2) {
+    extern __shared__ __align__(16) uint4 srec[];   // kTileRecs
+    __shared__ uint32_t hist[kWinMax], loff[kWinMax], s_warp[32];
+    __shared__ long long goff[kWinMax];
     __shared__ uint32_t s_lo, s_hi;
     const long n = min(long(*total), M);
-    const long tile = long(kWinTile) * blockDim.x;
-    for (long t0 = long(blockIdx.x) * tile; t0 < n; t0 += long(gridDim.x) * tile) {
+    for (long t0 = long(blockIdx.x) * kTileRecs; t0 < n; t0 += long(gridDim.x) * kTileRecs) {
         if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
         __syncthreads();
-        uint4 r[kWinTile];
+        uint4 r[kPlaceTile];
         uint32_t lo = 0xffffffffu, hi = 0u;
 #pragma unroll
-        for (int j = 0; j < kWinTile; ++j) {
-            const long i = t0 + long(j) * blockDim.x + threadIdx.x;
+        for (int j = 0; j < kPlaceTile; ++j) {
+            const long i = t0 + long(j) * kPlaceThreads + threadIdx.x;
             r[j] = i < n ? tmp[i] : make_uint4(0u, 0u, 0u, kNoBin);
             if (r[j].w != kNoBin) { lo = min(lo, r[j].w >> wshift); hi = max(hi, r[j].w >> wshift); }
         }
@@ -304,9 +358,8 @@ __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict_
         __syncthreads();
         const uint32_t wlo = s_lo, span = s_hi >= s_lo ? s_hi - s_lo + 1u : 0u;
         if (span > uint32_t(kWinMax)) {
-            // a tile across many sparse super-bins: one global atomic per record
 #pragma unroll
-            for (int j = 0; j < kWinTile; ++j) {
+            for (int j = 0; j < kPlaceTile; ++j) {
                 if (r[j].w == kNoBin) continue;
                 const uint32_t w = r[j].w >> wshift;
                 tmp2[qstart[w << wshift] + atomicAdd(&win_fill[w], 1u)] = r[j];
@@ -314,29 +367,40 @@ __global__ void __launch_bounds__(256) k_scatter_window(const uint4* __restrict_
             __syncthreads();
             continue;
         }
-        for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) hist[k] = 0u;
+        for (uint32_t k = threadIdx.x; k < span; k += kPlaceThreads) hist[k] = 0u;
         __syncthreads();
-        uint32_t lr[kWinTile];
+        uint32_t lr[kPlaceTile];
 #pragma unroll
-        for (int j = 0; j < kWinTile; ++j)
+        for (int j = 0; j < kPlaceTile; ++j)
             if (r[j].w != kNoBin) lr[j] = atomicAdd(&hist[(r[j].w >> wshift) - wlo], 1u);
         __syncthreads();
-        for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) {
-            const uint32_t c = hist[k];
-            if (c) hist[k] = qstart[(wlo + k) << wshift] + atomicAdd(&win_fill[wlo + k], c);
-        }
+        for (uint32_t k = threadIdx.x; k < span; k += kPlaceThreads) loff[k] = hist[k];
         __syncthreads();
+        const uint32_t ntile = block_scan_excl(loff, int(span), s_warp);
+        for (uint32_t k = threadIdx.x; k < span; k += kPlaceThreads) {
+            const uint32_t c = hist[k];
+            goff[k] = c ? (long long)(qstart[(wlo + k) << wshift] + atomicAdd(&win_fill[wlo + k], c)) - loff[k] : 0;
+        }
 #pragma unroll
-        for (int j = 0; j < kWinTile; ++j)
-            if (r[j].w != kNoBin) tmp2[hist[(r[j].w >> wshift) - wlo] + lr[j]] = r[j];
+        for (int j = 0; j < kPlaceTile; ++j)
+            if (r[j].w != kNoBin) srec[loff[(r[j].w >> wshift) - wlo] + lr[j]] = r[j];
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < ntile; i += kPlaceThreads) {
+            const uint4 q = srec[i];
+            tmp2[goff[(q.w >> wshift) - wlo] + i] = q;
+        }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(256) k_scatter_assemble(const uint4* __restrict__ tmp2, long nbins, int wshift,
-                                                           const uint32_t* __restrict__ qstart,
-                                                           const GridInst* __restrict__ inst, int n_inst,
-                                                           QRec* __restrict__ qrec) {
+// Pass 3: one window per CTA: every record gets its slot from shared-memory
+// counters started at qstart of its bin, the window is built in shared memory
+// and written out as one contiguous block (an over-full window stores
+// directly).
+__global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restrict__ tmp2, long nbins, int wshift,
+                                                            const uint32_t* __restrict__ qstart,
+                                                            const GridInst* __restrict__ inst, int n_inst,
+                                                            QRec* __restrict__ qrec) {
     extern __shared__ __align__(16) QRec buf[];   // kWinCap records
     __shared__ uint32_t cnt[kWinBinsMax];
     const long nwin = ((nbins - 1) >> wshift) + 1;
@@ -351,7 +415,7 @@ __global__ void __launch_bounds__(256) k_scatter_assemble(const uint4* __restric
             const uint32_t slot = atomicAdd(&cnt[r.w - uint32_t(b0)], 1u);
             const QRec q = make_qrec(r, inst, n_inst);
             if (fits) buf[slot - start] = q;
-            else qrec[slot] = q;   // an over-full window: direct stores
+            else qrec[slot] = q;
         }
         __syncthreads();
         if (fits)
@@ -1132,7 +1196,7 @@ void carve_queries(Carver& c, long nbins, long max_points, QueryBufs* q, bool tw
     q->qrec = c.take<QRec>(m);
     q->tmp = two_pass ? c.take<uint4>(m) : nullptr;
     q->tmp2 = two_pass ? c.take<uint4>(m) : nullptr;
-    q->super_fill = two_pass ? c.take<uint32_t>(kMaxSuper + 1) : nullptr;
+    q->super_fill = two_pass ? c.take<uint32_t>(kTargetSuper + 1) : nullptr;
     q->win_fill = two_pass ? c.take<uint32_t>(size_t(nbins + 1)) : nullptr;
     q->scan_tmp = c.take<uint32_t>(scan_tmp_elems(nbins + 1) + 1);
 }
@@ -1154,26 +1218,31 @@ int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
         int shift = 0;
         while (((g.nbins - 1) >> shift) + 1 > kTargetSuper) ++shift;
         const int nsuper = int(((g.nbins - 1) >> shift) + 1);
-        // windows of 2^W bins holding ~1024 samples on average
+        // windows of 2^W bins holding about half the assembly capacity on average
         const double per_bin = double(M) / double(std::max<long>(g.nbins, 1));
         int wshift = 0;
-        while (wshift < 10 && per_bin * double(2L << wshift) <= 1024.0) ++wshift;
+        while ((1 << (wshift + 1)) <= kWinBinsMax && per_bin * double(2L << wshift) <= 0.5 * kWinCap) ++wshift;
         const long nwin = ((g.nbins - 1) >> wshift) + 1;
         VPMC_CUDA(cudaMemsetAsync(q.super_fill, 0, sizeof(uint32_t) * size_t(nsuper), st));
         VPMC_CUDA(cudaMemsetAsync(q.win_fill, 0, sizeof(uint32_t) * size_t(nwin), st));
-        const long tiles = (M + long(kCoarseTile) * kCoarseThreads - 1) / (long(kCoarseTile) * kCoarseThreads);
-        VPMC_LAUNCH(k_scatter_coarse, int(std::max<long>(1, std::min<long>(tiles, 8L * ctx->sm_count))),
-                    kCoarseThreads, 0, st, pts, M, q.qbin, q.qstart, shift, nsuper, q.super_fill, q.tmp);
-        const long wtiles = (M + long(kWinTile) * 256 - 1) / (long(kWinTile) * 256);
-        VPMC_LAUNCH(k_scatter_window, int(std::max<long>(1, std::min<long>(wtiles, 8L * ctx->sm_count))), 256, 0, st,
-                    q.tmp, q.qstart + g.nbins, M, wshift, q.qstart, q.win_fill, q.tmp2);
         static bool configured[64] = {};
-        const size_t smem = sizeof(QRec) * size_t(kWinCap);
+        const size_t tile_smem = sizeof(uint4) * size_t(kTileRecs), win_smem = sizeof(QRec) * size_t(kWinCap);
         if (ctx->device < 64 && !configured[ctx->device]) {
-            VPMC_CUDA(cudaFuncSetAttribute(k_scatter_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            VPMC_CUDA(cudaFuncSetAttribute(k_scatter_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(tile_smem)));
+            VPMC_CUDA(cudaFuncSetAttribute(k_scatter_window, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(tile_smem)));
+            VPMC_CUDA(cudaFuncSetAttribute(k_scatter_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(win_smem)));
             configured[ctx->device] = true;
         }
-        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, 16L * ctx->sm_count))), 256, smem,
+        const long tiles = (M + kTileRecs - 1) / kTileRecs;
+        const int tgrid = int(std::max<long>(1, std::min<long>(tiles, 2L * ctx->sm_count)));
+        VPMC_LAUNCH(k_scatter_coarse, tgrid, kPlaceThreads, tile_smem, st, pts, M, q.qbin, q.qstart, shift, nsuper,
+                    q.super_fill, q.tmp);
+        VPMC_LAUNCH(k_scatter_window, tgrid, kPlaceThreads, tile_smem, st, q.tmp, q.qstart + g.nbins, M, wshift,
+                    q.qstart, q.win_fill, q.tmp2);
+        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, ctx->sm_count))), 1024, win_smem,
                     st, q.tmp2, g.nbins, wshift, q.qstart, g.inst, g.n_inst, q.qrec);
         return VPMC_OK;
     }
