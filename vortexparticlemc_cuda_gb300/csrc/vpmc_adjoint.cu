@@ -267,7 +267,7 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
     vpmc_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
-    VPMC_LAUNCH(k_adj_self, blocks_for(s->N), 256, 0, st, s->g.cand, s->g.perm, s->g.start, s->N,
+    VPMC_LAUNCH(k_adj_self, blocks_for(s->N), 256, 0, st, s->g.cand, s->g.perm, s->g.cstart, s->N,
                 uint32_t(s->g.nbins), A.selfq);
     VPMC_CUDA(cudaMemcpyAsync(lam_out, lam_in, 2 * sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
     VPMC_CUDA(cudaMemsetAsync(A.dcum, 0, 2 * sizeof(double) * size_t(s->n_inst), st));
@@ -302,10 +302,11 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         GridBufs gd = s->g;
         gd.start = s->q.qstart;
         gd.cand = A.dual;
-        VPMC_TRY(make_items(ctx, s->g, s->g.start, s->it, query_chunk(4)));
+        VPMC_TRY(make_items(ctx, s->g, s->g.cstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.dual_out, 0, 3 * sizeof(double) * size_t(s->N), st));
         EvalLaunch D;
         D.mode = unb ? EVAL_DUAL9_64 : EVAL_DUAL64;
+        D.rows = 1;   // the samples are grouped by whole bins
         D.qpt = 4;
         D.out_f64 = A.dual_out;
         VPMC_TRY(launch_eval(ctx, gd, A.selfq, s->it, D));

@@ -39,7 +39,7 @@ __device__ __forceinline__ int inst_of_bin(const GridInst* inst, int n_inst, uin
 __device__ __forceinline__ float wrapf(float p, float L) { return p - floorf(p / L) * L; }
 
 __global__ void k_grid_keys(const float2* __restrict__ pos, const float* __restrict__ omega, long n,
-                            const GridInst* __restrict__ inst, int n_inst, int set_mode, uint32_t nbins,
+                            const GridInst* __restrict__ inst, int n_inst, int set_mode, uint32_t nbins, int rows,
                             uint32_t* __restrict__ keys, uint32_t* __restrict__ count) {
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
         const GridInst G = inst[inst_of_particle(inst, n_inst, i)];
@@ -52,13 +52,16 @@ __global__ void k_grid_keys(const float2* __restrict__ pos, const float* __restr
             case SET_NEG_ONLY: use = w < 0.f; break;
             default: break;
         }
-        uint32_t key = nbins;
+        uint32_t key = nbins * uint32_t(rows);
         if (use) {
             float2 p = pos[i];
             if (G.periodic) { p.x = wrapf(p.x, G.Lx); p.y = wrapf(p.y, G.Ly); }
             const int cx = min(max(floor_int(p.x * G.inv_sx), 0), G.gx - 1);
             const int cy = min(max(floor_int(p.y * G.inv_sy), 0), G.gy - 1);
-            key = uint32_t(G.bin_base) + uint32_t(set) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
+            const uint32_t bin = uint32_t(G.bin_base) + uint32_t(set) * uint32_t(G.gx * G.gy) + uint32_t(cx * G.gy + cy);
+            // sub-row of the cell (nested: clamped into the cell's own rows)
+            const int r = min(max(floor_int(p.y * G.inv_sy * float(rows)) - cy * rows, 0), rows - 1);
+            key = bin * uint32_t(rows) + uint32_t(r);
             atomicAdd(&count[key], 1u);
         }
         keys[i] = key;
@@ -128,6 +131,12 @@ __global__ void k_sigma(const float4* __restrict__ F, long n, unsigned* __restri
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void k_coarse_starts(const uint32_t* __restrict__ start, long nbins, int rows,
+                                uint32_t* __restrict__ cstart) {
+    for (long b = long(blockIdx.x) * blockDim.x + threadIdx.x; b <= nbins; b += long(gridDim.x) * blockDim.x)
+        cstart[b] = start[b * rows];
 }
 
 __global__ void k_grid_weights(const double* __restrict__ x, long n, double scale, Cand* __restrict__ cand) {
@@ -463,7 +472,8 @@ struct BatchPiece {
 
 struct EvalArgs {
     const GridInst* inst;
-    const uint32_t* cstart;
+    const uint32_t* cstart;   // candidate range per sub-row (rows per cell: `rows`)
+    int rows;
     const Cand* cand;
     const CandF* candf;
     const QRec* qrec;
@@ -635,16 +645,24 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
             const uint32_t ncell = uint32_t(G.gx * G.gy);
             const uint32_t set = local / ncell, cell = local % ncell;
             const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
-            const uint32_t colbase = uint32_t(G.bin_base) + set * ncell;
+            const int R = a.rows, gyR = G.gy * R;
+            const uint32_t colbase = (uint32_t(G.bin_base) + set * ncell) * uint32_t(R);
             int np = 0;
             auto add = [&](int gxx, int r0, int r1, int sxi, int syi) {
                 if (r0 > r1) return;
-                const uint32_t b0 = colbase + uint32_t(gxx * G.gy + r0);
+                const uint32_t b0 = colbase + uint32_t(gxx * gyR + r0);
                 const uint32_t s = a.cstart[b0], e = a.cstart[b0 + uint32_t(r1 - r0) + 1];
                 if (e > s && np < kMaxPieces)
                     s_pc[np++] = Piece{s, e - s, -float(sxi) * G.Lx, -float(syi) * G.Ly, sxi, syi};
             };
+            const float sx = 1.f / G.inv_sx, reach2 = G.reach * G.reach;
             for (int ox = -G.k; ox <= G.k; ++ox) {
+                // the column is at least dx from every point of the bin's cell; its
+                // candidates within reach lie within dy = sqrt(reach^2 - dx^2) of the
+                // cell in y: sub-rows [cy R - m, cy R + R - 1 + m]
+                const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
+                if (dx * dx > reach2) continue;
+                const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * G.inv_sy * float(R) * 1.0001f)), G.k * R);
                 int gxx = cx + ox, sxi = 0;
                 if (G.periodic) {
                     if (gxx < 0) { gxx += G.gx; sxi = -1; }
@@ -652,19 +670,13 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                 } else if (gxx < 0 || gxx >= G.gx) {
                     continue;
                 }
-                // rows of this column that can hold a candidate within reach
-                // (reach <= k s): cell (ox, oy) is at least
-                // s sqrt((|ox|-1)^2 + (|oy|-1)^2) from every point of the bin's cell
-                const int ax = abs(ox) > 0 ? abs(ox) - 1 : 0;
-                int m = G.k;
-                while (m > 1 && ax * ax + (m - 1) * (m - 1) >= G.k * G.k) --m;
-                const int ylo = cy - m, yhi = cy + m;
+                const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
                 if (G.periodic) {
-                    if (ylo < 0) { add(gxx, 0, yhi, sxi, 0); add(gxx, ylo + G.gy, G.gy - 1, sxi, -1); }
-                    else if (yhi >= G.gy) { add(gxx, ylo, G.gy - 1, sxi, 0); add(gxx, 0, yhi - G.gy, sxi, 1); }
+                    if (ylo < 0) { add(gxx, 0, yhi, sxi, 0); add(gxx, ylo + gyR, gyR - 1, sxi, -1); }
+                    else if (yhi >= gyR) { add(gxx, ylo, gyR - 1, sxi, 0); add(gxx, 0, yhi - gyR, sxi, 1); }
                     else add(gxx, ylo, yhi, sxi, 0);
                 } else {
-                    add(gxx, max(ylo, 0), min(yhi, G.gy - 1), 0, 0);
+                    add(gxx, max(ylo, 0), min(yhi, gyR - 1), 0, 0);
                 }
             }
             s_np = np;
@@ -1098,6 +1110,7 @@ long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
         g.nsets = nsets;
         g.periodic = d.periodic;
         g.hw = d.hw;
+        g.reach = float(reach);
         const double h = d.hw;
         g.inv_hw = float(1.0 / h);
         g.A = float(3.0 / (h * h * h));
@@ -1112,19 +1125,22 @@ long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     return base;
 }
 
-void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed) {
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed, int rows) {
     g->inst = c.take<GridInst>(size_t(n_inst));
     g->n_inst = n_inst;
     g->nbins = nbins;
+    g->rows = rows < 1 ? 1 : rows;
     g->n = n;
+    const long nsub = nbins * g->rows;
     g->keys = c.take<uint32_t>(size_t(n < 1 ? 1 : n));
-    g->count = c.take<uint32_t>(size_t(nbins + 1));
-    g->start = c.take<uint32_t>(size_t(nbins + 1));
+    g->count = c.take<uint32_t>(size_t(nsub + 1));
+    g->start = c.take<uint32_t>(size_t(nsub + 1));
+    g->cstart = g->rows > 1 ? c.take<uint32_t>(size_t(nbins + 1)) : g->start;
     g->cand = c.take<Cand>(size_t(n < 1 ? 1 : n));
     g->candf = deformed ? c.take<CandF>(size_t(n < 1 ? 1 : n)) : nullptr;
     carve_radix(c, n, &g->rs);
     // the bin scan reuses the radix scan scratch when it is large enough
-    const size_t need = scan_tmp_elems(nbins + 1);
+    const size_t need = scan_tmp_elems(nsub + 1);
     if (need > scan_tmp_elems(long(radix_counts_elems(n)))) g->rs.scan_tmp = c.take<uint32_t>(need + 1);
 }
 
@@ -1132,19 +1148,22 @@ int grid_build(vpmc_context* ctx, GridBufs& g, const float2* pos, const float* o
                const float4* F) {
     if (F && !g.candf) return VPMC_ERR_INVALID;
     cudaStream_t st = ctx->stream;
-    VPMC_CUDA(cudaMemsetAsync(g.count, 0, sizeof(uint32_t) * size_t(g.nbins + 1), st));
+    const long nsub = g.nbins * g.rows;
+    VPMC_CUDA(cudaMemsetAsync(g.count, 0, sizeof(uint32_t) * size_t(nsub + 1), st));
     VPMC_LAUNCH(k_grid_keys, blocks_for(g.n), 256, 0, st, pos, omega, g.n, g.inst, g.n_inst, set_mode,
-                uint32_t(g.nbins), g.keys, g.count);
-    VPMC_TRY(exclusive_scan(ctx, g.count, g.start, g.nbins, g.rs.scan_tmp, true));
+                uint32_t(g.nbins), g.rows, g.keys, g.count);
+    VPMC_TRY(exclusive_scan(ctx, g.count, g.start, nsub, g.rs.scan_tmp, true));
     uint32_t *ks = nullptr, *vs = nullptr;
-    VPMC_TRY(radix_sort(ctx, g.keys, nullptr, g.n, bits_for(uint64_t(g.nbins) + 1), g.rs, &ks, &vs));
+    VPMC_TRY(radix_sort(ctx, g.keys, nullptr, g.n, bits_for(uint64_t(nsub) + 1), g.rs, &ks, &vs));
     g.perm = vs;
     if (F)
-        VPMC_LAUNCH(k_grid_gather_f, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega, F,
+        VPMC_LAUNCH(k_grid_gather_f, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(nsub), pos, omega, F,
                     g.inst, g.n_inst, set_mode, g.candf);
     else
-        VPMC_LAUNCH(k_grid_gather, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(g.nbins), pos, omega,
+        VPMC_LAUNCH(k_grid_gather, blocks_for(g.n), 256, 0, st, vs, g.start, g.n, uint32_t(nsub), pos, omega,
                     g.inst, g.n_inst, set_mode, g.cand);
+    if (g.rows > 1)
+        VPMC_LAUNCH(k_coarse_starts, blocks_for(g.nbins + 1), 256, 0, st, g.start, g.nbins, g.rows, g.cstart);
     return VPMC_OK;
 }
 
@@ -1260,7 +1279,8 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
     if (eval_deformed(L.mode) && !g.candf) return VPMC_ERR_INVALID;
-    EvalArgs a{g.inst, g.start, g.cand, g.candf, qrec, it.items, it.n_items, it.counter, L.out_f32, L.out_f64, ctx->d_flags};
+    EvalArgs a{g.inst, g.start, L.rows > 0 ? L.rows : g.rows, g.cand, g.candf, qrec, it.items, it.n_items, it.counter,
+               L.out_f32, L.out_f64, ctx->d_flags};
     switch (L.mode) {
         case EVAL_FIELD:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);

@@ -28,6 +28,7 @@ struct GridInst {
     int nsets;              // candidate sets (2 = sign split, 1 = one set)
     int periodic;
     float hw;               // support radius h_w
+    float reach;            // radius the walk must cover: h_w x cover (sigma_max of deformed kernels)
     float inv_hw;           // 1/h_w
     float A, B;             // 3/h_w^3, -3/h_w^2: W/(2 sigma) = min(0.5 + r^2 (A r + B), (1 - r/h_w)^3)
     float two_sigma;        // 2 * 40 / (7 pi h_w^2)
@@ -121,16 +122,18 @@ struct GridBufs {
     GridInst* inst = nullptr;   // device copy of the plan
     int n_inst = 0;
     long nbins = 0;
+    int rows = 1;               // candidate sub-rows per cell (candidates sorted by cell, then sub-row in y)
     long n = 0;                 // particles covered
     uint32_t* keys = nullptr;   // n
-    uint32_t* count = nullptr;  // nbins + 1
-    uint32_t* start = nullptr;  // nbins + 1 (exclusive prefix, start[nbins] = candidates)
+    uint32_t* count = nullptr;  // nbins * rows + 1
+    uint32_t* start = nullptr;  // nbins * rows + 1: candidate range of sub-row (bin * rows + r)
+    uint32_t* cstart = nullptr; // nbins + 1: candidate range of a whole bin (= start when rows == 1)
     Cand* cand = nullptr;       // n
     CandF* candf = nullptr;     // n (deformed kernels only)
     uint32_t* perm = nullptr;   // n: sorted slot -> particle (points into rs buffers)
     RadixScratch rs{};
 };
-void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed = false);
+void carve_grid(Carver& c, long n, long nbins, int n_inst, GridBufs* g, bool deformed = false, int rows = 1);
 
 // Bin keys + counts + stable sort + ranges + gather.  weights == nullptr uses
 // omega (SET_SIGN_SPLIT scales |omega| by 2 sigma, SET_ONE_SIGNED by
@@ -192,6 +195,7 @@ int grid_max_sigma(vpmc_context* ctx, const float4* F, long n, unsigned* d_words
 
 struct EvalLaunch {
     int mode = EVAL_FIELD;
+    int rows = -1;             // candidate sub-rows per cell of the candidate ranges (-1: the grid's)
     int qpt = 4;               // queries per thread (FIELD modes: 4 or 8; others: 4)
     float* out_f32 = nullptr;
     double* out_f64 = nullptr;

@@ -189,9 +189,9 @@ int vpmc_rbf_matvec(vpmc_context* ctx, int N, const float* pos, const float* x, 
     Work w;
     VPMC_TRY(setup(ctx, SLOT_CG, N, h_w, Lx, Ly, periodic, 0, 2, &w));
     VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), nullptr, SET_ONE_SIGNED));
-    VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.start, long(N),
+    VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.cstart, long(N),
                 uint32_t(w.g.nbins), 0, w.self);
-    VPMC_TRY(make_items(ctx, w.g, w.g.start, w.it, query_chunk(4)));
+    VPMC_TRY(make_items(ctx, w.g, w.g.cstart, w.it, query_chunk(4)));
     VPMC_LAUNCH(k_gather_to_sorted, blocks_for(N), 256, 0, st, x, w.g.perm, long(N), w.vec[0]);
     VPMC_TRY(spmv_sorted(ctx, w, w.vec[0], w.vec[1], precise != 0));
     VPMC_LAUNCH(k_scatter_from_sorted, blocks_for(N), 256, 0, st, w.vec[1], w.g.perm, long(N), y);
@@ -215,9 +215,9 @@ int cg_impl(vpmc_context* ctx, int N, const float* pos, const float* b, const do
     VPMC_TRY(setup(ctx, SLOT_CG, N, h_w, Lx, Ly, periodic, 0, 6, &w));
     double *bs = w.vec[0], *x = w.vec[1], *r = w.vec[2], *p = w.vec[3], *Ap = w.vec[4], *tmp = w.vec[5];
     VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), nullptr, SET_ONE_SIGNED));
-    VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.start, long(N),
+    VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.cstart, long(N),
                 uint32_t(w.g.nbins), 0, w.self);
-    VPMC_TRY(make_items(ctx, w.g, w.g.start, w.it, query_chunk(4)));
+    VPMC_TRY(make_items(ctx, w.g, w.g.cstart, w.it, query_chunk(4)));
     if (b64) VPMC_LAUNCH(k_gather_to_sorted_d, blocks_for(N), 256, 0, st, b64, w.g.perm, long(N), bs);
     else VPMC_LAUNCH(k_gather_to_sorted, blocks_for(N), 256, 0, st, b, w.g.perm, long(N), bs);
     const double diag = spline_w_d(0.0, double(h_w));   // W(0), the reference's x0 = b / W(0)

@@ -675,7 +675,7 @@ int alloc_work(vpmc_sim* s) {
     s->chunk_ev.assign(2 * nchunks, nullptr);
     for (auto& e : s->chunk_ev) VPMC_CUDA(cudaEventCreate(&e));
     auto carve_all = [&](Carver& c) {
-        carve_grid(c, s->N, nb, s->n_inst, &s->g, s->deform != 0);
+        carve_grid(c, s->N, nb, s->n_inst, &s->g, s->deform != 0, s->rows);
         carve_items(c, nb, ns, &s->it);
         carve_queries(c, nb, ns, &s->q, true);
         s->ys = c.take<float2>(size_t(ns));
