@@ -533,8 +533,8 @@ template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
                                            const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX],
                                            float A, float B, float ih) {
-    const f2x HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
-    const f2x A2 = pk2(A, A), B2 = pk2(B, B), NIH = pk2(-ih, -ih);
+    const f2x HALF = pk2(0.5f, 0.5f);
+    const f2x A2 = pk2(A, A), B2 = pk2(B, B);
 #pragma unroll 2
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
@@ -547,14 +547,17 @@ __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt,
             up2(r2p, ra, rb);
             // rounding can leave r^2 a hair below 0 when c ~ q: take sqrt(|r^2|);
             // the polynomial's r^2 term is then off by that hair only
-            const f2x r = pk2(sqrt_approx(fabsf(ra)), sqrt_approx(fabsf(rb)));
+            const float sa = sqrt_approx(fabsf(ra)), sb = sqrt_approx(fabsf(rb));
+            const f2x r = pk2(sa, sb);
             const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
-            const f2x t = fma2(NIH, r, ONE);
+            // t = max(1 - r/h, 0) by saturating FMAs (t <= 1 anyway): t^3 >= 0, and beyond
+            // the support min(inner, t^3) = 0 since inner > 0.5 there -- no max(., 0)
+            const f2x t = pk2(__saturatef(fmaf(-ih, sa, 1.f)), __saturatef(fmaf(-ih, sb, 1.f)));
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
             up2(in, ia, ib);
             up2(t3, ta, tb);
-            P[pr] = fma2(WC.x, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+            P[pr] = fma2(WC.x, pk2(fminf(ia, ta), fminf(ib, tb)), P[pr]);
         }
     }
 }
@@ -566,8 +569,8 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
                                              const f2x (&QXY)[NPMAX], const f2x (&QYY)[NPMAX],
                                              const f2x (&QX)[NPMAX], const f2x (&QY)[NPMAX], f2x (&P)[NPMAX],
                                              float A, float B, float ih) {
-    const f2x HALF = pk2(0.5f, 0.5f), ONE = pk2(1.f, 1.f);
-    const f2x A2 = pk2(A, A), B2 = pk2(B, B), NIH = pk2(-ih, -ih);
+    const f2x HALF = pk2(0.5f, 0.5f);
+    const f2x A2 = pk2(A, A), B2 = pk2(B, B);
 #pragma unroll 2
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2* rec = reinterpret_cast<const ulonglong2*>(cs[c].f);
@@ -584,14 +587,15 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
             r2p = fma2(R2.x, QY[pr], r2p);
             float ra, rb;
             up2(r2p, ra, rb);
-            const f2x r = pk2(sqrt_approx(fabsf(ra)), sqrt_approx(fabsf(rb)));
+            const float sa = sqrt_approx(fabsf(ra)), sb = sqrt_approx(fabsf(rb));
+            const f2x r = pk2(sa, sb);
             const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
-            const f2x t = fma2(NIH, r, ONE);
+            const f2x t = pk2(__saturatef(fmaf(-ih, sa, 1.f)), __saturatef(fmaf(-ih, sb, 1.f)));
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
             up2(in, ia, ib);
             up2(t3, ta, tb);
-            P[pr] = fma2(R3.x, pk2(fmaxf(fminf(ia, ta), 0.f), fmaxf(fminf(ib, tb), 0.f)), P[pr]);
+            P[pr] = fma2(R3.x, pk2(fminf(ia, ta), fminf(ib, tb)), P[pr]);
         }
     }
 }
