@@ -528,7 +528,8 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 // and c2 = x^2 + y^2; queries enter as -2 q and |q|^2, so
 //   r^2 = c2 + q2 - 2 c.q,  r = sqrt(|r^2|)
 //   P  += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)      (= w W / 2 sigma)
-// 9 FMA-pipe operations per pair (2 per query of r^2 setup, 1 sqrt on the XU).
+// Per pair of queries: 8 packed FMA-pipe operations + 2 saturating scalar FMAs,
+// 2 square roots on the XU and 2 min on the ALU.
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
                                            const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX],
