@@ -524,36 +524,35 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 }
 
 // Sum over one staged run of candidates for NPR packed query pairs, in
-// bin-local coordinates: candidates hold (x, y) relative to the bin centre
-// and c2 = x^2 + y^2; queries enter as -2 q and |q|^2, so
-//   r^2 = c2 + q2 - 2 c.q,  r = sqrt(|r^2|)
-//   P  += w * min(0.5 + r^2 (A r + B), max(1 - r/h, 0)^3)      (= w W / 2 sigma)
-// Per pair of queries: 8 packed FMA-pipe operations + 2 saturating scalar FMAs,
+// bin-local coordinates, every squared distance pre-scaled by kappa = -3/h^2:
+// candidates hold (x, y) relative to the bin centre and kappa c2; queries
+// enter as -2 kappa q and kappa |q|^2, so
+//   s2 = kappa c2 + kappa q2 - 2 kappa c.q = -3 (r/h)^2,   sqrt(|s2|) = sqrt(3) r/h
+//   t  = saturate(1 - sqrt(|s2|)/sqrt(3))                  (= max(1 - r/h, 0))
+//   P += w * min(0.5 + s2 t, t^3)                          (= w W / 2 sigma)
+// because the spline's inner branch 1/2 - 3 q^2 + 3 q^3 is 1/2 - 3 q^2 (1 - q),
+// and beyond the support t = 0 leaves min(1/2, 0) = 0.
+// Per pair of queries: 7 packed FMA-pipe operations + 2 saturating scalar FMAs,
 // 2 square roots on the XU and 2 min on the ALU.
+constexpr float kInvSqrt3 = 0.57735026918962576f;
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
-                                           const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX],
-                                           float A, float B, float ih) {
+                                           const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX]) {
     const f2x HALF = pk2(0.5f, 0.5f);
-    const f2x A2 = pk2(A, A), B2 = pk2(B, B);
 #pragma unroll 2
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
-        const ulonglong2 WC = *reinterpret_cast<const ulonglong2*>(&cs[c].w);   // (w, w), (c2, c2)
+        const ulonglong2 WC = *reinterpret_cast<const ulonglong2*>(&cs[c].w);   // (w, w), (kappa c2, kappa c2)
 #pragma unroll
         for (int pr = 0; pr < NPR; ++pr) {
             const f2x s = add2(WC.y, Q2[pr]);
-            const f2x r2p = fma2(XY.y, QY[pr], fma2(XY.x, QX[pr], s));
+            const f2x s2 = fma2(XY.y, QY[pr], fma2(XY.x, QX[pr], s));
             float ra, rb;
-            up2(r2p, ra, rb);
-            // rounding can leave r^2 a hair below 0 when c ~ q: take sqrt(|r^2|);
-            // the polynomial's r^2 term is then off by that hair only
+            up2(s2, ra, rb);
+            // rounding can leave s2 a hair above 0 when c ~ q: take sqrt(|s2|)
             const float sa = sqrt_approx(fabsf(ra)), sb = sqrt_approx(fabsf(rb));
-            const f2x r = pk2(sa, sb);
-            const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
-            // t = max(1 - r/h, 0) by saturating FMAs (t <= 1 anyway): t^3 >= 0, and beyond
-            // the support min(inner, t^3) = 0 since inner > 0.5 there -- no max(., 0)
-            const f2x t = pk2(__saturatef(fmaf(-ih, sa, 1.f)), __saturatef(fmaf(-ih, sb, 1.f)));
+            const f2x t = pk2(__saturatef(fmaf(-kInvSqrt3, sa, 1.f)), __saturatef(fmaf(-kInvSqrt3, sb, 1.f)));
+            const f2x in = fma2(s2, t, HALF);
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
             up2(in, ia, ib);
@@ -563,35 +562,32 @@ __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt,
     }
 }
 
-// The same sum for deformed kernels: r^2 from the expanded metric form
-// (5 packed FMAs instead of 3), the spline as above.
+// The same sum for deformed kernels: s2 from the expanded metric form, its
+// coefficients pre-scaled by kappa (5 packed FMAs instead of 3), the spline as above.
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int cnt, const f2x (&QXX)[NPMAX],
                                              const f2x (&QXY)[NPMAX], const f2x (&QYY)[NPMAX],
-                                             const f2x (&QX)[NPMAX], const f2x (&QY)[NPMAX], f2x (&P)[NPMAX],
-                                             float A, float B, float ih) {
+                                             const f2x (&QX)[NPMAX], const f2x (&QY)[NPMAX], f2x (&P)[NPMAX]) {
     const f2x HALF = pk2(0.5f, 0.5f);
-    const f2x A2 = pk2(A, A), B2 = pk2(B, B);
 #pragma unroll 2
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2* rec = reinterpret_cast<const ulonglong2*>(cs[c].f);
-        const ulonglong2 R0 = rec[0];   // (g11), (2 g12)
-        const ulonglong2 R1 = rec[1];   // (g22), (a)
-        const ulonglong2 R2 = rec[2];   // (b), (e)
+        const ulonglong2 R0 = rec[0];   // kappa (g11), kappa (2 g12)
+        const ulonglong2 R1 = rec[1];   // kappa (g22), kappa (a)
+        const ulonglong2 R2 = rec[2];   // kappa (b), kappa (e)
         const ulonglong2 R3 = rec[3];   // (w), (0)
 #pragma unroll
         for (int pr = 0; pr < NPR; ++pr) {
-            f2x r2p = fma2(R0.x, QXX[pr], R2.y);
-            r2p = fma2(R0.y, QXY[pr], r2p);
-            r2p = fma2(R1.x, QYY[pr], r2p);
-            r2p = fma2(R1.y, QX[pr], r2p);
-            r2p = fma2(R2.x, QY[pr], r2p);
+            f2x s2 = fma2(R0.x, QXX[pr], R2.y);
+            s2 = fma2(R0.y, QXY[pr], s2);
+            s2 = fma2(R1.x, QYY[pr], s2);
+            s2 = fma2(R1.y, QX[pr], s2);
+            s2 = fma2(R2.x, QY[pr], s2);
             float ra, rb;
-            up2(r2p, ra, rb);
+            up2(s2, ra, rb);
             const float sa = sqrt_approx(fabsf(ra)), sb = sqrt_approx(fabsf(rb));
-            const f2x r = pk2(sa, sb);
-            const f2x in = fma2(r2p, fma2(A2, r, B2), HALF);
-            const f2x t = pk2(__saturatef(fmaf(-ih, sa, 1.f)), __saturatef(fmaf(-ih, sb, 1.f)));
+            const f2x t = pk2(__saturatef(fmaf(-kInvSqrt3, sa, 1.f)), __saturatef(fmaf(-kInvSqrt3, sb, 1.f)));
+            const f2x in = fma2(s2, t, HALF);
             const f2x t3 = mul2(mul2(t, t), t);
             float ia, ib, ta, tb;
             up2(in, ia, ib);
@@ -601,8 +597,16 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
     }
 }
 
+// The packed FP32 kernels keep to 64 registers with 4 queries per thread (four
+// CTAs per SM: their 52 KB staging buffers fit four times in shared memory) and
+// to 128 with 8 (two CTAs per SM).
+constexpr int eval_min_blocks(int mode, int qpt) {
+    return (mode == EVAL_FIELD || mode == EVAL_FIELD9 || mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F)
+               ? (qpt == 4 ? 4 : 2) : 1;
+}
+
 template <int MODE, int QPT>
-__global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
+__global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_eval(EvalArgs a) {
     extern __shared__ __align__(128) Cand s_cand[];
     __shared__ Piece s_pc[kMaxPieces];
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
@@ -643,7 +647,11 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
         if (item >= *a.n_items) break;
         const Item it = a.items[item];
         const GridInst G = a.inst[it.inst];
-        const int nq = int((it.qcnt + kEvalThreads - 1) / kEvalThreads);   // queries per thread this item
+        // queries fill warps in order (warp w holds queries [w 32 QPT, (w + 1) 32 QPT) of the
+        // item, lane-interleaved), so a partly filled item leaves whole warps and whole
+        // packed pairs idle: npw = packed query pairs this warp evaluates (warp-uniform)
+        const int wbase = (tid >> 5) * 32 * QPT;
+        const int npw = (max(0, min(int(it.qcnt) - wbase, 32 * QPT)) + 63) >> 6;
 
         if (tid == 0) {
             const uint32_t local = it.bin - uint32_t(G.bin_base);
@@ -704,7 +712,7 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
         double accg[kGrad ? QPT : 1][2];
 #pragma unroll
         for (int j = 0; j < QPT; ++j) {
-            const uint32_t idx = uint32_t(tid + j * kEvalThreads);
+            const uint32_t idx = uint32_t(wbase + j * 32 + (tid & 31));
             qv[j] = idx < it.qcnt;
             QRec r = qv[j] ? a.qrec[it.qbeg + idx] : QRec{0.f, 0.f, 0u, (2u) | (2u << 3)};
             qx[j] = r.x;
@@ -755,7 +763,9 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
 
             const int nbp = s_nbp;
             if constexpr (kPacked) {
-                // staged candidates -> image-shifted, bin-local coordinates + c2
+                // staged candidates -> image-shifted, bin-local coordinates + kappa c2
+                // (kappa = -3/h^2 scales every squared distance, see packed_run)
+                const float kap = G.B;
                 for (int b = 0; b < nbp; ++b) {
                     const BatchPiece bp = s_bp[b];
                     const Piece pc = s_pc[bp.piece];
@@ -766,19 +776,19 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                             const float lx = f[0] - ox, ly = f[1] - oy;
                             const float g11 = f[2], g12 = f[3], g22 = f[4], w = f[5];
                             const float gx = fmaf(g11, lx, g12 * ly), gy = fmaf(g12, lx, g22 * ly);
-                            const float e = fmaf(lx, gx, ly * gy);
-                            f[0] = g11; f[1] = g11;
-                            f[2] = 2.f * g12; f[3] = 2.f * g12;
-                            f[4] = g22; f[5] = g22;
-                            f[6] = -2.f * gx; f[7] = -2.f * gx;
-                            f[8] = -2.f * gy; f[9] = -2.f * gy;
+                            const float e = kap * fmaf(lx, gx, ly * gy);
+                            f[0] = kap * g11; f[1] = f[0];
+                            f[2] = kap * (2.f * g12); f[3] = f[2];
+                            f[4] = kap * g22; f[5] = f[4];
+                            f[6] = kap * (-2.f * gx); f[7] = f[6];
+                            f[8] = kap * (-2.f * gy); f[9] = f[8];
                             f[10] = e; f[11] = e;
                             f[12] = w; f[13] = w;
                             f[14] = 0.f; f[15] = 0.f;
                         } else {
                             Cand& cd = s_cand[bp.soff + c];
                             const float lx = cd.x - ox, ly = cd.y - oy;
-                            const float c2 = fmaf(lx, lx, ly * ly);
+                            const float c2 = kap * fmaf(lx, lx, ly * ly);
                             cd.x = lx;
                             cd.x2 = lx;
                             cd.y = ly;
@@ -821,10 +831,10 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                         P[pr] = pk2(0.f, 0.f);
                     }
                     const CandF* csf = s_candf + bp.soff;
-                    if (nq <= 2) packed_run_f<1, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
-                    else if (NP >= 2 && nq <= 4)
-                        packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
-                    else packed_run_f<NP, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P, G.A, G.B, G.inv_hw);
+                    if (npw == 1) packed_run_f<1, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
+                    else if (NP >= 2 && npw == 2)
+                        packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
+                    else if (npw > 0) packed_run_f<NP, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;
@@ -833,21 +843,22 @@ __global__ void __launch_bounds__(kEvalThreads) k_eval(EvalArgs a) {
                         part[2 * pr + 1] = hi;
                     }
                 } else if constexpr (kPacked) {
-                    // queries in the same local frame: -2 q and |q|^2
+                    // queries in the same local frame: -2 kappa q and kappa |q|^2
                     f2x QX[NP], QY[NP], Q2[NP], P[NP];
+                    const float kap = G.B, m2k = -2.f * G.B;
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         const float ax = qx[2 * pr] - s_ox, bx = qx[2 * pr + 1] - s_ox;
                         const float ay = qy[2 * pr] - s_oy, by = qy[2 * pr + 1] - s_oy;
-                        QX[pr] = pk2(-2.f * ax, -2.f * bx);
-                        QY[pr] = pk2(-2.f * ay, -2.f * by);
-                        Q2[pr] = pk2(fmaf(ax, ax, ay * ay), fmaf(bx, bx, by * by));
+                        QX[pr] = pk2(m2k * ax, m2k * bx);
+                        QY[pr] = pk2(m2k * ay, m2k * by);
+                        Q2[pr] = pk2(kap * fmaf(ax, ax, ay * ay), kap * fmaf(bx, bx, by * by));
                         P[pr] = pk2(0.f, 0.f);
                     }
-                    // an item with few queries runs fewer pairs per thread (uniform per CTA)
-                    if (nq <= 2) packed_run<1, NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
-                    else if (NP >= 2 && nq <= 4) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
-                    else packed_run<NP, NP>(cs, cnt, QX, QY, Q2, P, G.A, G.B, G.inv_hw);
+                    // a warp with few queries runs fewer pairs (none when it holds no query)
+                    if (npw == 1) packed_run<1, NP>(cs, cnt, QX, QY, Q2, P);
+                    else if (NP >= 2 && npw == 2) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, Q2, P);
+                    else if (npw > 0) packed_run<NP, NP>(cs, cnt, QX, QY, Q2, P);
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;
