@@ -86,17 +86,30 @@ __global__ void k_identity(float4* __restrict__ F, long n) {
 
 // upper_bound(cdf[0..n), u) bracketed by a guide table of G = n entries:
 // guide[k] = upper_bound(k / G); result clamped to n-1 as the reference does.
+// u = u01d(r) = (2 r + 1) 2^-33 exactly.  The search runs on integers: for
+// non-negative doubles the IEEE bit patterns order as the values do, so
+// cdf[i] > u compares the 64-bit patterns (no FP64 instruction, the same index).
+// The guide slot is floor((2 r + 1) n / 2^33) in exact integer arithmetic; the
+// one-slot margin on both sides of the bracket covers the rounding of the
+// guide's own k / G.
+__device__ __forceinline__ unsigned long long u01d_bits(uint32_t r) {
+    const unsigned long long m = 2ull * r + 1ull;                 // 1 .. 2^33 - 1
+    const int p = 63 - __clzll(static_cast<long long>(m));        // leading bit
+    return (static_cast<unsigned long long>(1023 + p - 33) << 52) | ((m << (52 - p)) & ((1ull << 52) - 1ull));
+}
 __device__ __forceinline__ int sample_cdf(const double* __restrict__ cdf, const uint32_t* __restrict__ guide, int n,
-                                          double u) {
+                                          uint32_t r) {
     const int G = n;
-    int k = int(u * G);
+    const unsigned long long ub = u01d_bits(r);
+    int k = int(((2ull * r + 1ull) * static_cast<unsigned long long>(G)) >> 33);
     k = min(max(k, 0), G - 1);
     int lo = int(guide[max(k - 1, 0)]);
     int hi = int(guide[min(k + 2, G)]);   // guide[G] = n
+    const unsigned long long* cb = reinterpret_cast<const unsigned long long*>(cdf);
     // first index in [lo, hi) with cdf > u
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (cdf[mid] > u) hi = mid; else lo = mid + 1;
+        if (cb[mid] > ub) hi = mid; else lo = mid + 1;
     }
     return min(lo, n - 1);
 }
@@ -155,7 +168,7 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
             if (n == 0) {
                 valid = false;
             } else {
-                const int idx = sample_cdf(a.cdf + I.off[s], a.guide + I.goff[s], n, u01d(r.x));
+                const int idx = sample_cdf(a.cdf + I.off[s], a.guide + I.goff[s], n, r.x);
                 const int p = a.sub[I.off[s] + idx] + I.p_begin;   // subsets hold instance-local indices
                 src = p;
                 y = a.pos[p];
@@ -295,12 +308,24 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
         for (int s = 0; s < 2; ++s) {
             KSum sx, sy;
             const long base = (tl * 2 + s) * Q;
-            for (int j = lane; j < Q; j += 32) {
-                const float2 y = a.ys[base + j];
-                const float f = a.fv[base + j];
-                const float2 c = mis_term(I.law, x, y, f, w1, w2, I.cum9[s], alpha, R, I);
-                sx.add(c.x);
-                sy.add(c.y);
+            // four samples per lane in flight before their terms are summed (in
+            // the order j = lane, lane + 32, ...)
+            for (int j0 = lane; j0 < Q; j0 += 128) {
+                float2 y[4];
+                float f[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const int j = j0 + 32 * v;
+                    y[v] = j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
+                    f[v] = j < Q ? a.fv[base + j] : 0.f;
+                }
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    if (j0 + 32 * v >= Q) break;
+                    const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
+                    sx.add(c.x);
+                    sy.add(c.y);
+                }
             }
             u[s][0] = warp_sum_comp(sx.s, sx.c) * inv;
             u[s][1] = warp_sum_comp(sy.s, sy.c) * inv;
