@@ -410,21 +410,40 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
                                                             const uint32_t* __restrict__ qstart,
                                                             const GridInst* __restrict__ inst, int n_inst,
                                                             QRec* __restrict__ qrec) {
+    constexpr int kPer = kWinCap / 1024;            // records per thread of a window that fits
     extern __shared__ __align__(16) QRec buf[];   // kWinCap records
     __shared__ uint32_t cnt[kWinBinsMax];
     const long nwin = ((nbins - 1) >> wshift) + 1;
     for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
         const long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
         const uint32_t start = qstart[b0], nw = qstart[b1] - start;
+        const bool fits = nw <= uint32_t(kWinCap);
+        // the window's records are loaded together with its bin starts (one
+        // round trip), then slotted
+        uint4 r[kPer];
+        if (fits) {
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+                r[j] = k < nw ? tmp2[start + k] : make_uint4(0u, 0u, 0u, 0u);
+            }
+        }
         for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) cnt[b - b0] = qstart[b];
         __syncthreads();
-        const bool fits = nw <= uint32_t(kWinCap);
-        for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) {
-            const uint4 r = tmp2[start + k];
-            const uint32_t slot = atomicAdd(&cnt[r.w - uint32_t(b0)], 1u);
-            const QRec q = make_qrec(r, inst, n_inst);
-            if (fits) buf[slot - start] = q;
-            else qrec[slot] = q;
+        if (fits) {
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+                if (k >= nw) break;
+                const uint32_t slot = atomicAdd(&cnt[r[j].w - uint32_t(b0)], 1u);
+                buf[slot - start] = make_qrec(r[j], inst, n_inst);
+            }
+        } else {
+            for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) {
+                const uint4 rr = tmp2[start + k];
+                const uint32_t slot = atomicAdd(&cnt[rr.w - uint32_t(b0)], 1u);
+                qrec[slot] = make_qrec(rr, inst, n_inst);
+            }
         }
         __syncthreads();
         if (fits)
@@ -636,15 +655,17 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         mbar_init(&s_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
+        s_item = atomicAdd(a.counter, 1u);
     }
     __syncthreads();
     uint32_t phase = 0;
 
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(a.counter, 1u);
-        __syncthreads();
         const uint32_t item = s_item;
         if (item >= *a.n_items) break;
+        // claim the next item now: the atomic's round trip hides behind this one
+        uint32_t next_item = 0;
+        if (tid == 0) next_item = atomicAdd(a.counter, 1u);
         const Item it = a.items[item];
         const GridInst G = a.inst[it.inst];
         // queries fill warps in order (warp w holds queries [w 32 QPT, (w + 1) 32 QPT) of the
@@ -653,53 +674,78 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         const int wbase = (tid >> 5) * 32 * QPT;
         const int npw = (max(0, min(int(it.qcnt) - wbase, 32 * QPT)) + 63) >> 6;
 
-        if (tid == 0) {
+        if (tid < 32) {
+            // the walk, one column per lane of warp 0 (2 k + 1 <= 17 columns): each
+            // column gives up to two runs (a periodic column wrapping in y splits),
+            // emitted in column order as a serial walk would
+            const int lane = tid;
             const uint32_t local = it.bin - uint32_t(G.bin_base);
             const uint32_t ncell = uint32_t(G.gx * G.gy);
             const uint32_t set = local / ncell, cell = local % ncell;
             const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
             const int R = a.rows, gyR = G.gy * R;
             const uint32_t colbase = (uint32_t(G.bin_base) + set * ncell) * uint32_t(R);
-            int np = 0;
-            auto add = [&](int gxx, int r0, int r1, int sxi, int syi) {
-                if (r0 > r1) return;
-                const uint32_t b0 = colbase + uint32_t(gxx * gyR + r0);
-                const uint32_t s = a.cstart[b0], e = a.cstart[b0 + uint32_t(r1 - r0) + 1];
-                if (e > s && np < kMaxPieces)
-                    s_pc[np++] = Piece{s, e - s, -float(sxi) * G.Lx, -float(syi) * G.Ly, sxi, syi};
-            };
             const float sx = 1.f / G.inv_sx, reach2 = G.reach * G.reach;
-            for (int ox = -G.k; ox <= G.k; ++ox) {
-                // the column is at least dx from every point of the bin's cell; its
-                // candidates within reach lie within dy = sqrt(reach^2 - dx^2) of the
-                // cell in y: sub-rows [cy R - m, cy R + R - 1 + m]
-                const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
-                if (dx * dx > reach2) continue;
-                // (1e-3 of a sub-row of tolerance: the pairs it can skip lie within 0.2% of
-                // the kernel's support edge, where W / W(0) < 1e-7)
-                const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * G.inv_sy * float(R) - 1e-3f)), G.k * R);
-                int gxx = cx + ox, sxi = 0;
+            const int ox = lane - G.k;
+            int gxx = cx + ox, sxi = 0;
+            int r0[2] = {1, 1}, r1[2] = {0, 0}, syi[2] = {0, 0};   // empty unless set below
+            // the column is at least dx from every point of the bin's cell; its
+            // candidates within reach lie within dy = sqrt(reach^2 - dx^2) of the
+            // cell in y: sub-rows [cy R - m, cy R + R - 1 + m]
+            const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
+            bool col = ox <= G.k && dx * dx <= reach2;
+            if (col) {
                 if (G.periodic) {
                     if (gxx < 0) { gxx += G.gx; sxi = -1; }
                     else if (gxx >= G.gx) { gxx -= G.gx; sxi = 1; }
                 } else if (gxx < 0 || gxx >= G.gx) {
-                    continue;
-                }
-                const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
-                if (G.periodic) {
-                    if (ylo < 0) { add(gxx, 0, yhi, sxi, 0); add(gxx, ylo + gyR, gyR - 1, sxi, -1); }
-                    else if (yhi >= gyR) { add(gxx, ylo, gyR - 1, sxi, 0); add(gxx, 0, yhi - gyR, sxi, 1); }
-                    else add(gxx, ylo, yhi, sxi, 0);
-                } else {
-                    add(gxx, max(ylo, 0), min(yhi, gyR - 1), 0, 0);
+                    col = false;
                 }
             }
-            s_np = np;
-            s_cur_piece = 0;
-            s_cur_off = 0;
-            // bin centre (wrapped coordinates): origin of the local frame
-            s_ox = (float(cx) + 0.5f) / G.inv_sx;
-            s_oy = (float(cy) + 0.5f) / G.inv_sy;
+            if (col) {
+                // (1e-3 of a sub-row of tolerance: the pairs it can skip lie within 0.2% of
+                // the kernel's support edge, where W / W(0) < 1e-7)
+                const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * G.inv_sy * float(R) - 1e-3f)), G.k * R);
+                const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
+                if (G.periodic) {
+                    if (ylo < 0) {
+                        r0[0] = 0; r1[0] = yhi;
+                        r0[1] = ylo + gyR; r1[1] = gyR - 1; syi[1] = -1;
+                    } else if (yhi >= gyR) {
+                        r0[0] = ylo; r1[0] = gyR - 1;
+                        r0[1] = 0; r1[1] = yhi - gyR; syi[1] = 1;
+                    } else {
+                        r0[0] = ylo; r1[0] = yhi;
+                    }
+                } else {
+                    r0[0] = max(ylo, 0); r1[0] = min(yhi, gyR - 1);
+                }
+            }
+            uint32_t rs[2] = {0u, 0u}, re[2] = {0u, 0u};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (r0[h] <= r1[h]) {
+                    const uint32_t b0 = colbase + uint32_t(gxx * gyR + r0[h]);
+                    rs[h] = a.cstart[b0];
+                    re[h] = a.cstart[b0 + uint32_t(r1[h] - r0[h]) + 1];
+                }
+            }
+            const bool v0 = re[0] > rs[0], v1 = re[1] > rs[1];
+            const unsigned m0 = __ballot_sync(0xffffffffu, v0), m1 = __ballot_sync(0xffffffffu, v1);
+            const unsigned lt = (1u << lane) - 1u;
+            const int pos = __popc(m0 & lt) + __popc(m1 & lt);   // <= 2 (2 k + 1) = kMaxPieces
+            if (v0) s_pc[pos] = Piece{rs[0], re[0] - rs[0], -float(sxi) * G.Lx, -float(syi[0]) * G.Ly, sxi, syi[0]};
+            if (v1)
+                s_pc[pos + (v0 ? 1 : 0)] =
+                    Piece{rs[1], re[1] - rs[1], -float(sxi) * G.Lx, -float(syi[1]) * G.Ly, sxi, syi[1]};
+            if (lane == 0) {
+                s_np = __popc(m0) + __popc(m1);
+                s_cur_piece = 0;
+                s_cur_off = 0;
+                // bin centre (wrapped coordinates): origin of the local frame
+                s_ox = (float(cx) + 0.5f) / G.inv_sx;
+                s_oy = (float(cy) + 0.5f) / G.inv_sy;
+            }
         }
 
         // this thread's queries
@@ -1059,6 +1105,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             else if constexpr (kComp) a.out_f64[qid[j]] = double(acc[j]) - double(acc_c[j]);
             else a.out_f32[qid[j]] = acc[j];
         }
+        if (tid == 0) s_item = next_item;
         __syncthreads();
     }
     if (s_abort) {
