@@ -292,8 +292,16 @@ def run_gpu(args, wl):
         # the plain FP64 GPU path of the same estimator (the comparison baseline of the FP32 path)
         sim.set_precision(64)
 
-    # accuracy at the fixed sample count: velocity RMS error vs the FP64 direct
-    # sum at 4096 random particles (seed 2)
+    if args.k or args.qpt or args.precision == 64:
+        sim.set_tuning(args.k or 4, args.qpt or 4)   # FP64: no autotuning passes (seconds each)
+    else:
+        t_t = time.perf_counter()
+        k_sel, q_sel, best = sim.autotune()
+        tune = {"k_walk": k_sel, "queries_per_thread": q_sel, "best_pass_ms": best,
+                "seconds": time.perf_counter() - t_t}
+        log(f"autotune: {tune}")
+    # accuracy at the fixed sample count, with the tuning the timed steps use:
+    # velocity RMS error vs the FP64 direct sum at 4096 random particles (seed 2)
     err = None
     if args.err_queries > 0:
         n0 = counts[0]   # instance 0
@@ -314,14 +322,6 @@ def run_gpu(args, wl):
             err["instance"] = 0
 
     log(f"accuracy: {err}")
-    if args.k or args.qpt or args.precision == 64:
-        sim.set_tuning(args.k or 4, args.qpt or 4)   # FP64: no autotuning passes (seconds each)
-    else:
-        t_t = time.perf_counter()
-        k_sel, q_sel, best = sim.autotune()
-        tune = {"k_walk": k_sel, "queries_per_thread": q_sel, "best_pass_ms": best,
-                "seconds": time.perf_counter() - t_t}
-        log(f"autotune: {tune}")
     geo = sim.geometry()
     sim.set_step(0)
     sim.step(args.warmup, use_graph=True)

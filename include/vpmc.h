@@ -379,8 +379,11 @@ int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
  * candidate (k_walk, queries_per_thread) in {2,3,4,6,8}x{4} + {2,3,4}x{8}, keeps
  * the fastest, and caches the choice in-process by (hwr, samples per target,
  * particles per h_w^2).  Results do not depend on the choice beyond FP32
- * rounding of the field sums.  Outputs (HOST, may be NULL): chosen k,
- * queries per thread, and the best pass time in ms (-1 when cached). */
+ * rounding of the field sums, and the autotuner checks that: each
+ * candidate's sum of |u|^2 over the targets must agree with the candidates'
+ * median to 1e-4 (relative), else VPMC_ERR_DEVICE (a kernel variant gave
+ * different results).  Outputs (HOST, may be NULL): chosen k, queries per
+ * thread, and the best pass time in ms (-1 when cached). */
 int vpmc_sim_autotune(vpmc_sim* sim, int* k_walk, int* queries_per_thread, float* best_ms);
 
 /* Kernels launched per step by the last captured or eager pass, and the

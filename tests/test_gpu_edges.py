@@ -69,3 +69,21 @@ def test_ensemble_with_an_empty_member_and_a_tiny_domain(cuda):
     solo.prepare()
     solo.step(2)
     assert np.array_equal(solo.particles()[0].cpu().numpy(), p[: len(a)])
+
+
+def test_context_closed_before_its_simulation(cuda):
+    """A simulation holds a reference to its context: closing the context
+    first (as a garbage collector may) leaves the simulation usable and its
+    own close safe."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    pos = O.lattice(16)
+    om = (O.taylor_green(pos) * np.float32(1e-3)).astype(np.float32)
+    ctx = P.Context()
+    sim = P.Simulation(P.SimParam(dt=1e-3, Nx=16, hwr=2, N1=8, N2=8, law=P.LAW_UNBIASED, seed=1), [len(pos)],
+                       ctx=ctx)
+    sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+    sim.prepare()
+    ctx.close()                       # the creator lets go first
+    sim.step(1)
+    assert np.isfinite(sim.particles()[0].cpu().numpy()).all()
+    sim.close()                       # the last holder frees the context

@@ -14,6 +14,18 @@ static thread_local char g_last_error[512] = {0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int context_release(vpmc_context* c) {
+    if (c->refs.fetch_sub(1) > 1) return VPMC_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& b : c->scratch) b.release();
+    if (c->d_flags) cudaFree(c->d_flags);
+    if (c->h_flags) cudaFreeHost(c->h_flags);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return VPMC_OK;
+}
+
 void record_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
     std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file,
                   line);
@@ -136,15 +148,9 @@ int vpmc_context_create(int device, void* stream, vpmc_context** out) {
 
 int vpmc_context_destroy(vpmc_context* c) {
     if (!c) return VPMC_ERR_INVALID;
-    cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto& b : c->scratch) b.release();
-    if (c->d_flags) cudaFree(c->d_flags);
-    if (c->h_flags) cudaFreeHost(c->h_flags);
-    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
-    delete c;
-    return VPMC_OK;
+    return vpmc::context_release(c);
 }
+
 
 void* vpmc_context_stream(vpmc_context* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
 

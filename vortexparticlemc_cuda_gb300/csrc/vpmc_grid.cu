@@ -14,7 +14,7 @@ namespace {
 constexpr int kEvalThreads = 256;
 constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
-constexpr int kCandCap = 1664;                 // candidates staged per batch (52 KB: 4 CTAs per SM)
+constexpr int kCandCap = 1600;                 // candidates staged per batch (50 KB: 4 CTAs per SM)
 constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
@@ -337,6 +337,20 @@ __device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ 
     return QRec{p.x, p.y, r.z, fl};
 }
 
+// Sub-cell of a query (wrapped point p in the cell of bin `bin`): 4 x 4
+// sub-cells in serpentine order (rows of sub-cells, alternate rows reversed),
+// so that any run of consecutive keys covers a compact part of the cell.
+constexpr int kSubCells = 16;
+__device__ __forceinline__ uint32_t subcell_key(float px, float py, uint32_t bin, const GridInst* __restrict__ inst,
+                                                int n_inst) {
+    const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, bin)];
+    const uint32_t cell = (bin - uint32_t(G.bin_base)) % uint32_t(G.gx * G.gy);
+    const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
+    const int ix = min(max(int((px * G.inv_sx - float(cx)) * 4.f), 0), 3);
+    const int iy = min(max(int((py * G.inv_sy - float(cy)) * 4.f), 0), 3);
+    return uint32_t(iy * 4 + ((iy & 1) ? 3 - ix : ix));
+}
+
 // Pass 2: the same per tile of the super-bin-grouped records, by window
 // (2^W consecutive bins), placed from the window's first slot qstart[w << W].
 // A tile spanning more windows than the shared-memory counters hold (one
@@ -413,6 +427,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
     constexpr int kPer = kWinCap / 1024;            // records per thread of a window that fits
     extern __shared__ __align__(16) QRec buf[];   // kWinCap records
     __shared__ uint32_t cnt[kWinBinsMax];
+    __shared__ uint32_t sub[kSubCells * kWinBinsMax];   // per (sub-cell, bin of the window): count, then first slot
     const long nwin = ((nbins - 1) >> wshift) + 1;
     for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
         const long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
@@ -428,15 +443,41 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
                 r[j] = k < nw ? tmp2[start + k] : make_uint4(0u, 0u, 0u, 0u);
             }
         }
+        const uint32_t nb = uint32_t(b1 - b0);
         for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) cnt[b - b0] = qstart[b];
+        for (uint32_t i = threadIdx.x; i < uint32_t(kSubCells) * nb; i += blockDim.x) sub[i] = 0u;
         __syncthreads();
         if (fits) {
+            // inside each bin the records are ordered by sub-cell, so that
+            // consecutive queries of a bin lie close together
+            uint32_t kr[kPer];   // bin in the window | sub-cell << 8 | rank within (sub-cell, bin) << 12
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
                 const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
                 if (k >= nw) break;
-                const uint32_t slot = atomicAdd(&cnt[r[j].w - uint32_t(b0)], 1u);
-                buf[slot - start] = make_qrec(r[j], inst, n_inst);
+                const uint32_t bl = r[j].w - uint32_t(b0);
+                const QRec q = make_qrec(r[j], inst, n_inst);
+                const uint32_t key = subcell_key(q.x, q.y, r[j].w, inst, n_inst);
+                kr[j] = bl | (key << 8) | (atomicAdd(&sub[key * nb + bl], 1u) << 12);
+                r[j] = make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), q.id, q.flags);
+            }
+            __syncthreads();
+            for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+                uint32_t off = cnt[b];
+#pragma unroll
+                for (int c = 0; c < kSubCells; ++c) {
+                    const uint32_t n = sub[uint32_t(c) * nb + b];
+                    sub[uint32_t(c) * nb + b] = off;
+                    off += n;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+                if (k >= nw) break;
+                const uint32_t slot = sub[((kr[j] >> 8) & 15u) * nb + (kr[j] & 255u)] + (kr[j] >> 12);
+                buf[slot - start] = QRec{__uint_as_float(r[j].x), __uint_as_float(r[j].y), r[j].z, r[j].w};
             }
         } else {
             for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) {
@@ -482,7 +523,10 @@ __global__ void k_items_fill(const uint32_t* __restrict__ qstart, long nbins, in
 struct Piece {
     uint32_t gstart, cnt;   // candidate run in global memory
     float qdx, qdy;         // offset added to the query point (folds the periodic image)
-    int mx, my;             // image index of the run (for FIELD9)
+    uint32_t b0;            // index into the sub-row starts of the run's first sub-row
+    float x0, y0;           // bin-local left edge of the run's column, lower edge of its first sub-row
+    int16_t nr;             // sub-rows in the run
+    int8_t mx, my;          // image index of the run (for FIELD9)
 };
 struct BatchPiece {
     uint32_t soff, cnt, gstart;
@@ -629,6 +673,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     extern __shared__ __align__(128) Cand s_cand[];
     __shared__ Piece s_pc[kMaxPieces];
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
+    __shared__ uint2 s_rng[kEvalThreads / 32][kMaxPieces + 2];   // per warp: its part of each batch piece
+    __shared__ float4 s_wb[kEvalThreads / 32];                    // per warp: query bounding box (x0, x1, y0, y1)
     __shared__ int s_np, s_nbp, s_cur_piece, s_abort;
     __shared__ uint32_t s_cur_off, s_btot, s_item;
     __shared__ float s_ox, s_oy;
@@ -734,24 +780,40 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             const unsigned m0 = __ballot_sync(0xffffffffu, v0), m1 = __ballot_sync(0xffffffffu, v1);
             const unsigned lt = (1u << lane) - 1u;
             const int pos = __popc(m0 & lt) + __popc(m1 & lt);   // <= 2 (2 k + 1) = kMaxPieces
-            if (v0) s_pc[pos] = Piece{rs[0], re[0] - rs[0], -float(sxi) * G.Lx, -float(syi[0]) * G.Ly, sxi, syi[0]};
-            if (v1)
-                s_pc[pos + (v0 ? 1 : 0)] =
-                    Piece{rs[1], re[1] - rs[1], -float(sxi) * G.Lx, -float(syi[1]) * G.Ly, sxi, syi[1]};
+            // bin centre (wrapped coordinates): origin of the local frame
+            const float ocx = (float(cx) + 0.5f) / G.inv_sx, ocy = (float(cy) + 0.5f) / G.inv_sy;
+            const float srow = 1.f / (G.inv_sy * float(R));
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (!(h == 0 ? v0 : v1)) continue;
+                Piece pc;
+                pc.gstart = rs[h];
+                pc.cnt = re[h] - rs[h];
+                pc.qdx = -float(sxi) * G.Lx;
+                pc.qdy = -float(syi[h]) * G.Ly;
+                pc.b0 = colbase + uint32_t(gxx * gyR + r0[h]);
+                pc.x0 = float(gxx) / G.inv_sx - ocx - pc.qdx;
+                pc.y0 = float(r0[h]) * srow - ocy - pc.qdy;
+                pc.nr = int16_t(r1[h] - r0[h] + 1);
+                pc.mx = int8_t(sxi);
+                pc.my = int8_t(syi[h]);
+                s_pc[pos + (h == 1 && v0 ? 1 : 0)] = pc;
+            }
             if (lane == 0) {
                 s_np = __popc(m0) + __popc(m1);
                 s_cur_piece = 0;
                 s_cur_off = 0;
-                // bin centre (wrapped coordinates): origin of the local frame
-                s_ox = (float(cx) + 0.5f) / G.inv_sx;
-                s_oy = (float(cy) + 0.5f) / G.inv_sy;
+                s_ox = ocx;
+                s_oy = ocy;
             }
         }
 
         // this thread's queries
         float qx[QPT], qy[QPT];
         uint32_t qid[QPT];
-        int qmx[QPT], qmy[QPT];
+        // image flags of the queries, 6 bits each (FIELD9)
+        using QFlags = typename std::conditional<(6 * QPT > 32), unsigned long long, uint32_t>::type;
+        QFlags qfl = 0;
         bool qv[QPT];
         Acc acc[QPT];
         float acc_c[QPT];
@@ -764,13 +826,32 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             qx[j] = r.x;
             qy[j] = r.y;
             qid[j] = r.id;
-            qmx[j] = int(r.flags & 7u) - 2;
-            qmy[j] = int((r.flags >> 3) & 7u) - 2;
+            qfl |= QFlags(r.flags & 63u) << (6 * j);
             acc[j] = Acc(0);
             acc_c[j] = 0.f;
             if constexpr (kGrad) accg[j][0] = accg[j][1] = 0.0;
         }
         __syncthreads();
+        if constexpr (kPacked) {
+            // bounding box of this warp's queries in the bin's frame
+            float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY;
+#pragma unroll
+            for (int j = 0; j < QPT; ++j) {
+                if (!qv[j]) continue;
+                bx0 = fminf(bx0, qx[j]);
+                bx1 = fmaxf(bx1, qx[j]);
+                by0 = fminf(by0, qy[j]);
+                by1 = fmaxf(by1, qy[j]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+                bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+                by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+                by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+            }
+            if ((tid & 31) == 0) s_wb[tid >> 5] = make_float4(bx0 - s_ox, bx1 - s_ox, by0 - s_oy, by1 - s_oy);
+        }
 
         for (;;) {
             if (tid == 0) {
@@ -802,6 +883,38 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             }
             __syncthreads();
             if (s_btot == 0) break;
+            if constexpr (kPacked) {
+                // this warp's part of each staged run: the sub-rows within reach of
+                // its queries' bounding box (reach widened by 0.1%, sub-row bounds by
+                // 1% of a sub-row, so no pair with a non-zero term is dropped: the
+                // sums equal those over the whole runs).  The sub-row starts are read
+                // while the bulk copy is in flight.
+                if (npw > 0) {
+                    const int wid = tid >> 5;
+                    const float4 bb = s_wb[wid];
+                    const float sxw = 1.f / G.inv_sx, inv_srow = G.inv_sy * float(a.rows);
+                    const float rm = G.reach * 1.001f;
+                    for (int b = tid & 31; b < s_nbp; b += 32) {
+                        const BatchPiece bp = s_bp[b];
+                        const Piece pc = s_pc[bp.piece];
+                        uint32_t lo = 0u, hi = 0u;
+                        const float dxw = fmaxf(0.f, fmaxf(pc.x0 - bb.y, bb.x - (pc.x0 + sxw)));
+                        if (dxw < rm) {
+                            const float dy = sqrtf(fmaf(rm, rm, -dxw * dxw));
+                            const int ilo = max(int(floorf(fmaf(bb.z - dy - pc.y0, inv_srow, -0.01f))), 0);
+                            const int ihi = min(int(floorf(fmaf(bb.w + dy - pc.y0, inv_srow, 0.01f))), int(pc.nr) - 1);
+                            if (ilo <= ihi) {
+                                const uint32_t t0 = a.cstart[pc.b0 + uint32_t(ilo)];
+                                const uint32_t t1 = a.cstart[pc.b0 + uint32_t(ihi) + 1u];
+                                const uint32_t g0 = bp.gstart, g1 = bp.gstart + bp.cnt;
+                                lo = min(max(t0, g0), g1) - g0;
+                                hi = max(min(max(t1, g0), g1) - g0, lo);
+                            }
+                        }
+                        s_rng[wid][b] = make_uint2(lo, hi);
+                    }
+                }
+            }
             if (!mbar_wait_bounded(&s_bar, phase, kWaitLimit)) atomicOr(&s_abort, 1);
             phase ^= 1u;
             __syncthreads();
@@ -850,9 +963,11 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 const BatchPiece bp = s_bp[b];
                 const Piece pc = s_pc[bp.piece];
                 int cnt = int(bp.cnt);
+                const int bfirst = b;
                 if constexpr (kPacked) {
                     // staged runs sit back to back in shared memory, already in the
-                    // bin's frame: consecutive runs under the same image mask are one sweep
+                    // bin's frame: consecutive runs under the same image mask are one
+                    // sweep (each warp visits its own part of each run, in run order)
                     while (b + 1 < nbp) {
                         const Piece nx = s_pc[s_bp[b + 1].piece];
                         if (kField9 && (nx.mx != pc.mx || nx.my != pc.my)) break;
@@ -876,11 +991,16 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         QY[pr] = pk2(ay, by);
                         P[pr] = pk2(0.f, 0.f);
                     }
-                    const CandF* csf = s_candf + bp.soff;
-                    if (npw == 1) packed_run_f<1, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
-                    else if (NP >= 2 && npw == 2)
-                        packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
-                    else if (npw > 0) packed_run_f<NP, NP>(csf, cnt, QXX, QXY, QYY, QX, QY, P);
+                    for (int gb = bfirst; gb <= b && npw > 0; ++gb) {
+                        const uint2 rg = s_rng[tid >> 5][gb];
+                        const int n = int(rg.y) - int(rg.x);
+                        if (n <= 0) continue;
+                        const CandF* csf = s_candf + s_bp[gb].soff + rg.x;
+                        if (npw == 1) packed_run_f<1, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
+                        else if (NP >= 2 && npw == 2)
+                            packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
+                        else packed_run_f<NP, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
+                    }
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;
@@ -902,9 +1022,15 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         P[pr] = pk2(0.f, 0.f);
                     }
                     // a warp with few queries runs fewer pairs (none when it holds no query)
-                    if (npw == 1) packed_run<1, NP>(cs, cnt, QX, QY, Q2, P);
-                    else if (NP >= 2 && npw == 2) packed_run<(NP >= 2 ? 2 : 1), NP>(cs, cnt, QX, QY, Q2, P);
-                    else if (npw > 0) packed_run<NP, NP>(cs, cnt, QX, QY, Q2, P);
+                    for (int gb = bfirst; gb <= b && npw > 0; ++gb) {
+                        const uint2 rg = s_rng[tid >> 5][gb];
+                        const int n = int(rg.y) - int(rg.x);
+                        if (n <= 0) continue;
+                        const Cand* c0 = s_cand + s_bp[gb].soff + rg.x;
+                        if (npw == 1) packed_run<1, NP>(c0, n, QX, QY, Q2, P);
+                        else if (NP >= 2 && npw == 2) packed_run<(NP >= 2 ? 2 : 1), NP>(c0, n, QX, QY, Q2, P);
+                        else packed_run<NP, NP>(c0, n, QX, QY, Q2, P);
+                    }
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         float lo, hi;
@@ -953,7 +1079,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         pv[j] = pgx[j] = pgy[j] = 0.0;
                         use[j] = true;
                         if (MODE == EVAL_GRAD9_64) {
-                            const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
+                            const int mx = int(uint32_t(qfl >> (6 * j)) & 7u) - 2 + pc.mx;
+                            const int my = int(uint32_t(qfl >> (6 * j + 3)) & 7u) - 2 + pc.my;
                             use[j] = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
                         }
                     }
@@ -1075,7 +1202,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 for (int j = 0; j < QPT && !kGrad; ++j) {
                     bool use = true;
                     if (kField9) {
-                        const int mx = qmx[j] + pc.mx, my = qmy[j] + pc.my;
+                        const int mx = int(uint32_t(qfl >> (6 * j)) & 7u) - 2 + pc.mx;
+                        const int my = int(uint32_t(qfl >> (6 * j + 3)) & 7u) - 2 + pc.my;
                         use = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
                     }
                     if (use) {

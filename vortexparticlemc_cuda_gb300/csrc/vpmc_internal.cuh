@@ -84,10 +84,16 @@ struct vpmc_context {
     vpmc::DevBuf scratch[vpmc::kScratchSlots];
     unsigned* d_flags = nullptr;   // device error flags
     unsigned* h_flags = nullptr;   // pinned mirror
+    // holders: the creator plus every simulation bound to the context; the
+    // context is freed when the last one lets go (so destroying a context
+    // before its simulations, as a garbage collector may, stays safe)
+    std::atomic<int> refs{1};
 };
 
 namespace vpmc {
 
+// Drop one holder of the context; the last one frees it.
+int context_release(vpmc_context* ctx);
 // Read and clear the device flag word (synchronises the stream).
 int collect_flags(vpmc_context* ctx);
 // Reserve a scratch slot of at least `bytes` and return its base.

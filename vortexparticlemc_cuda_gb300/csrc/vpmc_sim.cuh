@@ -133,6 +133,7 @@ struct vpmc_sim {
     float4* F = nullptr;
     float4* F_next = nullptr;
     unsigned* d_sig = nullptr;         // 2 words
+    double* d_check = nullptr;         // autotuner: sum of |u|^2 of a pass
     // adjoint: checkpointed forward record and working set
     bool frozen = false;               // prepare keeps the sampling CDF, refreshes only Omega
     bool prepared_once = false;

@@ -284,7 +284,7 @@ class Simulation:
     """Simulation (include/vortex_particle_mc.hpp:136-192) over one or more
     independent instances (an ensemble), each with its own SimParam."""
 
-    def __init__(self, params, counts, device: int | None = None):
+    def __init__(self, params, counts, device: int | None = None, ctx: Context | None = None):
         if isinstance(params, SimParam):
             params = [params]
         counts = list(counts)
@@ -292,7 +292,7 @@ class Simulation:
             raise ValueError("one particle count per instance")
         self.params = list(params)
         self.counts = counts
-        self.ctx = context(device)
+        self.ctx = ctx if ctx is not None else context(device)
         arr = (SimParams * len(params))(*[p.c() for p in params])
         cnt = (C.c_int * len(counts))(*counts)
         h = C.c_void_p()
