@@ -281,7 +281,7 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         const long nt = std::min(s->chunk_targets, s->N - t0);
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
-        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
+        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, nullptr, nullptr, s->sub, s->cdf, s->guide, s->jit, s->d_step, t0,
                    nt, s->N1, s->N2, 1, A.src, s->ys, s->q.qbin, s->q.qcount, s->q.tmp ? nullptr : s->q.qrank};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
         VPMC_TRY(scatter_ranked(ctx, s->g, s->q, s->ys, ns));

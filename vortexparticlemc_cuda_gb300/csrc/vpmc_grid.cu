@@ -11,10 +11,10 @@ namespace vpmc {
 
 namespace {
 
-constexpr int kEvalThreads = 256;
+constexpr int kEvalThreads = 128;
 constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
-constexpr int kCandCap = 1600;                 // candidates staged per batch (50 KB: 4 CTAs per SM)
+constexpr int kCandCap = 768;                  // candidates staged per batch (24 KB: 8 CTAs per SM)
 constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
@@ -231,8 +231,8 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 //     flags) and writes it out as one contiguous block.
 // The order of queries inside a bin is not fixed by this; no result depends
 // on it (each query's field value is its own fixed-order sum).
-constexpr int kPlaceThreads = 256;
-constexpr int kPlaceTile = 16;                               // records per thread per tile
+constexpr int kPlaceThreads = 512;
+constexpr int kPlaceTile = 8;                                // records per thread per tile
 constexpr int kTileRecs = kPlaceThreads * kPlaceTile;        // 4096 records = 64 KB staged per tile
 constexpr int kTargetSuper = 256;                            // super-bins per grid
 constexpr int kWinMax = 2048;                                // windows one tile may sort in shared memory
@@ -660,12 +660,12 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
     }
 }
 
-// The packed FP32 kernels keep to 64 registers with 4 queries per thread (four
-// CTAs per SM: their 52 KB staging buffers fit four times in shared memory) and
-// to 128 with 8 (two CTAs per SM).
+// The packed FP32 kernels keep to 64 registers with 4 queries per thread (eight
+// CTAs of 128 threads per SM: their 24 KB staging buffers fit eight times in
+// shared memory) and to 128 with 8 (four CTAs per SM).
 constexpr int eval_min_blocks(int mode, int qpt) {
     return (mode == EVAL_FIELD || mode == EVAL_FIELD9 || mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F)
-               ? (qpt == 4 ? 4 : 2) : 1;
+               ? (qpt == 4 ? 8 : 4) : 1;
 }
 
 template <int MODE, int QPT>
@@ -714,11 +714,14 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         if (tid == 0) next_item = atomicAdd(a.counter, 1u);
         const Item it = a.items[item];
         const GridInst G = a.inst[it.inst];
-        // queries fill warps in order (warp w holds queries [w 32 QPT, (w + 1) 32 QPT) of the
-        // item, lane-interleaved), so a partly filled item leaves whole warps and whole
-        // packed pairs idle: npw = packed query pairs this warp evaluates (warp-uniform)
-        const int wbase = (tid >> 5) * 32 * QPT;
-        const int npw = (max(0, min(int(it.qcnt) - wbase, 32 * QPT)) + 63) >> 6;
+        // the item's queries form units of 64 (one packed pair per lane); the warps
+        // take consecutive units, as evenly as the count allows (a partly filled
+        // item leaves no warp idle while another holds two units more), and a
+        // warp runs only the pairs it holds: npw = its units (warp-uniform)
+        constexpr int kWarps = kEvalThreads / 32;
+        const int nunits = (int(it.qcnt) + 63) >> 6;   // <= kWarps * QPT / 2
+        const int u0 = ((tid >> 5) * nunits) / kWarps;
+        const int npw = (((tid >> 5) + 1) * nunits) / kWarps - u0;
 
         if (tid < 32) {
             // the walk, one column per lane of warp 0 (2 k + 1 <= 17 columns): each
@@ -820,8 +823,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         double accg[kGrad ? QPT : 1][2];
 #pragma unroll
         for (int j = 0; j < QPT; ++j) {
-            const uint32_t idx = uint32_t(wbase + j * 32 + (tid & 31));
-            qv[j] = idx < it.qcnt;
+            const uint32_t idx = uint32_t((u0 + (j >> 1)) * 64 + (j & 1) * 32 + (tid & 31));
+            qv[j] = (j >> 1) < npw && idx < it.qcnt;
             QRec r = qv[j] ? a.qrec[it.qbeg + idx] : QRec{0.f, 0.f, 0u, (2u) | (2u << 3)};
             qx[j] = r.x;
             qy[j] = r.y;

@@ -85,7 +85,9 @@ __global__ void k_identity(float4* __restrict__ F, long n) {
 }
 
 // upper_bound(cdf[0..n), u) bracketed by a guide table of G = n entries:
-// guide[k] = upper_bound(k / G); result clamped to n-1 as the reference does.
+// guide(j) = upper_bound(j / G), guide(G) = n; result clamped to n-1 as the
+// reference does.  Slot k of the table holds the bracket
+// (guide(max(k - 1, 0)), guide(min(k + 2, G))): one 8-byte load.
 // u = u01d(r) = (2 r + 1) 2^-33 exactly.  The search runs on integers: for
 // non-negative doubles the IEEE bit patterns order as the values do, so
 // cdf[i] > u compares the 64-bit patterns (no FP64 instruction, the same index).
@@ -97,14 +99,14 @@ __device__ __forceinline__ unsigned long long u01d_bits(uint32_t r) {
     const int p = 63 - __clzll(static_cast<long long>(m));        // leading bit
     return (static_cast<unsigned long long>(1023 + p - 33) << 52) | ((m << (52 - p)) & ((1ull << 52) - 1ull));
 }
-__device__ __forceinline__ int sample_cdf(const double* __restrict__ cdf, const uint32_t* __restrict__ guide, int n,
+__device__ __forceinline__ int sample_cdf(const double* __restrict__ cdf, const uint2* __restrict__ bracket, int n,
                                           uint32_t r) {
     const int G = n;
     const unsigned long long ub = u01d_bits(r);
     int k = int(((2ull * r + 1ull) * static_cast<unsigned long long>(G)) >> 33);
     k = min(max(k, 0), G - 1);
-    int lo = int(guide[max(k - 1, 0)]);
-    int hi = int(guide[min(k + 2, G)]);   // guide[G] = n
+    const uint2 b = bracket[k];
+    int lo = int(b.x), hi = int(b.y);
     const unsigned long long* cb = reinterpret_cast<const unsigned long long*>(cdf);
     // first index in [lo, hi) with cdf > u
     while (lo < hi) {
@@ -114,15 +116,32 @@ __device__ __forceinline__ int sample_cdf(const double* __restrict__ cdf, const 
     return min(lo, n - 1);
 }
 
-__global__ void k_guide(const double* __restrict__ cdf, int n, uint32_t* __restrict__ guide) {
-    for (long k = long(blockIdx.x) * blockDim.x + threadIdx.x; k <= n; k += long(gridDim.x) * blockDim.x) {
-        const double v = double(k) / double(n);
-        int lo = 0, hi = n;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (cdf[mid] > v) hi = mid; else lo = mid + 1;
-        }
-        guide[k] = uint32_t(k == n ? n : lo);
+__device__ __forceinline__ int guide_at(const double* __restrict__ cdf, int n, long j) {
+    if (j >= n) return n;
+    const double v = double(j) / double(n);
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] > v) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+__global__ void k_guide(const double* __restrict__ cdf, int n, uint2* __restrict__ bracket) {
+    for (long k = long(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += long(gridDim.x) * blockDim.x)
+        bracket[k] = make_uint2(uint32_t(guide_at(cdf, n, k > 0 ? k - 1 : 0)), uint32_t(guide_at(cdf, n, k + 2)));
+}
+
+// Positions in subset order (plain method): pos_sub[e] = pos of subset entry e,
+// so a branch-1 draw reads its source in one load.  Entries past a subset's
+// count are left alone.
+__global__ void k_sub_pos(const InstMC* __restrict__ mc, int n_inst, const int* __restrict__ sub,
+                          const float2* __restrict__ pos, long n2, float2* __restrict__ pos_sub) {
+    for (long e = long(blockIdx.x) * blockDim.x + threadIdx.x; e < n2; e += long(gridDim.x) * blockDim.x) {
+        const InstMC& I = mc[inst_of(mc, n_inst, e >> 1)];
+        const bool in0 = e >= I.off[0] && e - I.off[0] < I.cnt[0];
+        const bool in1 = e >= I.off[1] && e - I.off[1] < I.cnt[1];
+        if (in0 || in1) pos_sub[e] = pos[sub[e] + I.p_begin];
     }
 }
 
@@ -169,9 +188,14 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                 valid = false;
             } else {
                 const int idx = sample_cdf(a.cdf + I.off[s], a.guide + I.goff[s], n, r.x);
-                const int p = a.sub[I.off[s] + idx] + I.p_begin;   // subsets hold instance-local indices
-                src = p;
-                y = a.pos[p];
+                int p = -1;
+                if (a.pos_sub) {
+                    y = a.pos_sub[I.off[s] + idx];
+                } else {
+                    p = a.sub[I.off[s] + idx] + I.p_begin;   // subsets hold instance-local indices
+                    src = p;
+                    y = a.pos[p];
+                }
                 if (I.periodic) {
                     const int m9 = min(int(u01(r.y) * 9.f), 8);
                     y.x += float(m9 / 3 - 1) * I.Lx;
@@ -190,7 +214,8 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                     const float f = ur * kJitTab;
                     const int i0 = min(int(f), kJitTab - 1);
                     const float tt = f - i0;
-                    rr = (a.jit[i0] * (1.f - tt) + a.jit[i0 + 1] * tt) * I.hw;
+                    const float2 jt = a.jit[i0];   // (table[i0], table[i0 + 1])
+                    rr = (jt.x * (1.f - tt) + jt.y * tt) * I.hw;
                 }
                 float sn, cs;
                 sincosf(2.f * kPiF * u01(r.w), &sn, &cs);
@@ -284,10 +309,13 @@ __device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f,
     }
     const float r2 = rx * rx + ry * ry;
     if (!(r2 > 0.f)) return make_float2(0.f, 0.f);
+    // K(x - y) f / (w1 f / cum + w2 p2(|x - y|)), p2 = alpha / r inside the disk:
+    // multiplied through by cum r, one division per term
+    //   sc = f cum r / ((w1 f r + w2 alpha cum) 2 pi r^2)   (inside)
+    //   sc = cum / (w1 2 pi r^2)                             (outside)
     const float rn = sqrtf(r2);
-    const float p2 = rn < R ? alpha / rn : 0.f;
-    const float denom = w1 * f / cum + w2 * p2;
-    const float sc = f / (denom * (2.f * kPiF * r2));
+    const float tpr2 = 2.f * kPiF * r2;
+    const float sc = rn < R ? (f * cum * rn) / (fmaf(w1 * f, rn, w2 * alpha * cum) * tpr2) : cum / (w1 * tpr2);
     return make_float2(-ry * sc, rx * sc);
 }
 
@@ -776,11 +804,14 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT, def ? s->F : nullptr));
     if (def && advect) VPMC_CUDA(cudaMemsetAsync(s->d_sig, 0, 2 * sizeof(unsigned), st));
     const long Q = samples_per(s);
+    if (!def) VPMC_LAUNCH(k_sub_pos, blocks_for(2 * s->N), 256, 0, st, s->d_mc, s->n_inst, s->sub, s->pos, 2 * s->N,
+                          s->pos_sub);
     for (long t0 = 0; t0 < s->N; t0 += s->chunk_targets) {
         const long nt = std::min(s->chunk_targets, s->N - t0);
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
-        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, def ? s->F : nullptr, s->sub, s->cdf, s->guide, s->jit,
+        GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, def ? s->F : nullptr, def ? nullptr : s->pos_sub, s->sub,
+                   s->cdf, s->guide, s->jit,
                    s->d_step, t0, nt, s->N1, s->N2, def ? 5 : 1, nullptr, s->ys, s->q.qbin, s->q.qcount,
                    s->q.tmp ? nullptr : s->q.qrank};
         VPMC_LAUNCH(k_gen, blocks_for(ns), 256, 0, st, ga);
@@ -949,8 +980,9 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
         s->omega = c.take<float>(size_t(N));
         s->sub = c.take<int>(2 * size_t(N) + 2);
         s->cdf = c.take<double>(2 * size_t(N) + 2);
-        s->guide = c.take<uint32_t>(size_t(N) + 4 * size_t(n_inst) + 4);
-        s->jit = c.take<float>(kJitTab + 2);
+        s->guide = c.take<uint2>(size_t(N) + 4 * size_t(n_inst) + 4);
+        s->jit = c.take<float2>(kJitTab + 1);
+        s->pos_sub = c.take<float2>(2 * size_t(N) + 2);
         s->d_mc = c.take<InstMC>(size_t(n_inst));
         s->d_step = c.take<unsigned long long>(1);
         s->F = c.take<float4>(size_t(N));
@@ -967,7 +999,9 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
     build_jitter_table(jt);
     cudaStream_t st = ctx->stream;
     cudaMemsetAsync(s->mem.p, 0, s->mem.bytes, st);
-    cudaMemcpyAsync(s->jit, jt.data(), sizeof(float) * jt.size(), cudaMemcpyHostToDevice, st);
+    std::vector<float2> jt2(kJitTab);
+    for (int i = 0; i < kJitTab; ++i) jt2[i] = make_float2(jt[i], jt[i + 1]);
+    cudaMemcpyAsync(s->jit, jt2.data(), sizeof(float2) * jt2.size(), cudaMemcpyHostToDevice, st);
     unsigned long long zero = 0;
     cudaMemcpyAsync(s->d_step, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
     k_identity<<<blocks_for(N), 256, 0, st>>>(s->F, N);
@@ -1082,7 +1116,7 @@ int vpmc_sim_prepare(vpmc_sim* s) {
         for (int sg = 0; sg < 2; ++sg) {
             m.goff[sg] = goff;
             if (cnt[sg] > 0 && !(s->frozen && s->prepared_once))
-                VPMC_LAUNCH(k_guide, blocks_for(cnt[sg] + 1), 256, 0, st, s->cdf + m.off[sg], cnt[sg], s->guide + goff);
+                VPMC_LAUNCH(k_guide, blocks_for(cnt[sg]), 256, 0, st, s->cdf + m.off[sg], cnt[sg], s->guide + goff);
             goff += cnt[sg] + 2;
         }
     }

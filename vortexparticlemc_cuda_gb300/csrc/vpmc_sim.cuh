@@ -54,10 +54,11 @@ struct GenArgs {
     const GridInst* gi;
     const float2* pos;
     const float4* F;              // deformation mode: per-particle F (branch-1 jitter F r); else nullptr
+    const float2* pos_sub;        // positions in subset order, or nullptr (then sub + pos)
     const int* sub;
     const double* cdf;
-    const uint32_t* guide;
-    const float* jit;             // kJitTab+1 entries: inverse spline-radius CDF (units of h_w)
+    const uint2* guide;           // CDF search brackets per guide slot
+    const float2* jit;            // kJitTab pairs (t[i], t[i+1]) of the inverse spline-radius CDF (units of h_w)
     const unsigned long long* step;
     long t0, nt;                  // target chunk
     int N1, N2;
@@ -107,8 +108,9 @@ struct vpmc_sim {
     float* omega = nullptr;
     int* sub = nullptr;                // instance i: positives at 2*b_i, negatives at 2*b_i + n_i
     double* cdf = nullptr;
-    uint32_t* guide = nullptr;
-    float* jit = nullptr;
+    uint2* guide = nullptr;            // CDF search brackets (see k_guide)
+    float2* jit = nullptr;             // paired jitter table
+    float2* pos_sub = nullptr;         // positions in subset order (plain method)
     InstMC* d_mc = nullptr;
     unsigned long long* d_step = nullptr;
     std::vector<InstMC> mc;
