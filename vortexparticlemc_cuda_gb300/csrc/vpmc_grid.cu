@@ -337,17 +337,14 @@ __device__ __forceinline__ QRec make_qrec(uint4 r, const GridInst* __restrict__ 
     return QRec{p.x, p.y, r.z, fl};
 }
 
-// Sub-cell of a query (wrapped point p in the cell of bin `bin`): 4 x 4
+// Sub-cell of a query (wrapped point p in the cell of its bin): 4 x 4
 // sub-cells in serpentine order (rows of sub-cells, alternate rows reversed),
 // so that any run of consecutive keys covers a compact part of the cell.
+// c = {cx, cy, gx / Lx, gy / Ly} of the bin's cell.
 constexpr int kSubCells = 16;
-__device__ __forceinline__ uint32_t subcell_key(float px, float py, uint32_t bin, const GridInst* __restrict__ inst,
-                                                int n_inst) {
-    const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, bin)];
-    const uint32_t cell = (bin - uint32_t(G.bin_base)) % uint32_t(G.gx * G.gy);
-    const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
-    const int ix = min(max(int((px * G.inv_sx - float(cx)) * 4.f), 0), 3);
-    const int iy = min(max(int((py * G.inv_sy - float(cy)) * 4.f), 0), 3);
+__device__ __forceinline__ uint32_t subcell_key(float px, float py, float4 c) {
+    const int ix = min(max(int((px * c.z - c.x) * 4.f), 0), 3);
+    const int iy = min(max(int((py * c.w - c.y) * 4.f), 0), 3);
     return uint32_t(iy * 4 + ((iy & 1) ? 3 - ix : ix));
 }
 
@@ -428,6 +425,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
     extern __shared__ __align__(16) QRec buf[];   // kWinCap records
     __shared__ uint32_t cnt[kWinBinsMax];
     __shared__ uint32_t sub[kSubCells * kWinBinsMax];   // per (sub-cell, bin of the window): count, then first slot
+    __shared__ float4 corg[kWinBinsMax];                 // per bin of the window: its cell, for subcell_key
     const long nwin = ((nbins - 1) >> wshift) + 1;
     for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
         const long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
@@ -444,7 +442,12 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
             }
         }
         const uint32_t nb = uint32_t(b1 - b0);
-        for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) cnt[b - b0] = qstart[b];
+        for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+            cnt[b - b0] = qstart[b];
+            const GridInst& G = inst[n_inst == 1 ? 0 : inst_of_bin(inst, n_inst, uint32_t(b))];
+            const uint32_t cell = (uint32_t(b) - uint32_t(G.bin_base)) % uint32_t(G.gx * G.gy);
+            corg[b - b0] = make_float4(float(int(cell) / G.gy), float(int(cell) % G.gy), G.inv_sx, G.inv_sy);
+        }
         for (uint32_t i = threadIdx.x; i < uint32_t(kSubCells) * nb; i += blockDim.x) sub[i] = 0u;
         __syncthreads();
         if (fits) {
@@ -457,7 +460,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
                 if (k >= nw) break;
                 const uint32_t bl = r[j].w - uint32_t(b0);
                 const QRec q = make_qrec(r[j], inst, n_inst);
-                const uint32_t key = subcell_key(q.x, q.y, r[j].w, inst, n_inst);
+                const uint32_t key = subcell_key(q.x, q.y, corg[bl]);
                 kr[j] = bl | (key << 8) | (atomicAdd(&sub[key * nb + bl], 1u) << 12);
                 r[j] = make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), q.id, q.flags);
             }
@@ -675,7 +678,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
     __shared__ uint2 s_rng[kEvalThreads / 32][kMaxPieces + 2];   // per warp: its part of each batch piece
     __shared__ float4 s_wb[kEvalThreads / 32];                    // per warp: query bounding box (x0, x1, y0, y1)
-    __shared__ int s_np, s_nbp, s_cur_piece, s_abort;
+    __shared__ int s_np, s_nbp, s_cur_piece, s_abort, s_pre;
     __shared__ uint32_t s_cur_off, s_btot, s_item;
     __shared__ float s_ox, s_oy;
     __shared__ __align__(8) uint64_t s_bar;
@@ -802,10 +805,44 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 pc.my = int8_t(syi[h]);
                 s_pc[pos + (h == 1 && v0 ? 1 : 0)] = pc;
             }
+            // a walk that fits one batch is planned and its bulk copies issued here,
+            // by the lanes that hold its runs (the previous item's reads of the
+            // staging buffer ended at the item's closing barrier)
+            const uint32_t c0 = v0 ? re[0] - rs[0] : 0u, c1 = v1 ? re[1] - rs[1] : 0u;
+            uint32_t incl = c0 + c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const uint32_t tot_all = __shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t ex = incl - c0 - c1;   // staging offset of this lane's first run
+            const bool one = tot_all > 0u && tot_all <= uint32_t(kCap);
+            const int np = __popc(m0) + __popc(m1);
+            if (one) {
+                if (v0) s_bp[pos] = BatchPiece{ex, c0, rs[0], pos};
+                if (v1) s_bp[pos + (v0 ? 1 : 0)] = BatchPiece{ex + c0, c1, rs[1], pos + (v0 ? 1 : 0)};
+                if (lane == 0) {
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(&s_bar, tot_all * kRec);
+                }
+                __syncwarp();
+                fence_proxy_async_smem();
+                const char* gsrc = kDef ? reinterpret_cast<const char*>(a.candf) : reinterpret_cast<const char*>(a.cand);
+                if (v0)
+                    bulk_g2s(reinterpret_cast<char*>(s_cand) + size_t(ex) * kRec, gsrc + size_t(rs[0]) * kRec,
+                             c0 * kRec, &s_bar);
+                if (v1)
+                    bulk_g2s(reinterpret_cast<char*>(s_cand) + size_t(ex + c0) * kRec, gsrc + size_t(rs[1]) * kRec,
+                             c1 * kRec, &s_bar);
+            }
             if (lane == 0) {
-                s_np = __popc(m0) + __popc(m1);
-                s_cur_piece = 0;
+                s_np = np;
+                s_cur_piece = one ? np : 0;
                 s_cur_off = 0;
+                s_pre = one ? 1 : 0;
+                s_nbp = one ? np : 0;
+                s_btot = one ? tot_all : 0u;
                 s_ox = ocx;
                 s_oy = ocy;
             }
@@ -857,6 +894,9 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         }
 
         for (;;) {
+            // s_pre: this batch was planned and issued with the walk (read after a
+            // barrier, cleared by thread 0 once every thread is past the next one)
+            if (!s_pre) {
             if (tid == 0) {
                 // next batch: whole or partial pieces up to the staging capacity
                 int pc = s_cur_piece;
@@ -885,6 +925,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 }
             }
             __syncthreads();
+            }
             if (s_btot == 0) break;
             if constexpr (kPacked) {
                 // this warp's part of each staged run: the sub-rows within reach of
@@ -918,10 +959,15 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                     }
                 }
             }
+            // each thread sees the copied bytes once its own wait completes; the
+            // packed modes rewrite them first, so their barrier follows that pass
             if (!mbar_wait_bounded(&s_bar, phase, kWaitLimit)) atomicOr(&s_abort, 1);
             phase ^= 1u;
-            __syncthreads();
-            if (s_abort) break;
+            if constexpr (!kPacked) {
+                __syncthreads();
+                if (tid == 0) s_pre = 0;
+                if (s_abort) break;
+            }
 
             const int nbp = s_nbp;
             if constexpr (kPacked) {
@@ -961,6 +1007,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                     }
                 }
                 __syncthreads();
+                if (tid == 0) s_pre = 0;
+                if (s_abort) break;   // (a thread whose wait expired rewrote stale bytes: unused)
             }
             for (int b = 0; b < nbp; ++b) {
                 const BatchPiece bp = s_bp[b];
@@ -1222,6 +1270,9 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                     }
                 }
             }
+            // no further batch in this item: the item's closing barrier guards the
+            // staging buffer (the cursor only moves in the next planning step)
+            if (s_cur_piece >= s_np) break;
             __syncthreads();   // all reads of s_cand done before the next batch overwrites it
         }
         if (s_abort) break;
