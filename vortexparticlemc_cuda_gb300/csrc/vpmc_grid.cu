@@ -599,13 +599,14 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 // because the spline's inner branch 1/2 - 3 q^2 + 3 q^3 is 1/2 - 3 q^2 (1 - q),
 // and beyond the support t = 0 leaves min(1/2, 0) = 0.
 // Per pair of queries: 7 packed FMA-pipe operations + 2 saturating scalar FMAs,
-// 2 square roots on the XU and 2 min on the ALU.
+// 2 square roots on the XU and 2 min on the ALU.  The candidate loop is unrolled
+// four times (independent chains across candidates; still 64 registers).
 constexpr float kInvSqrt3 = 0.57735026918962576f;
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
                                            const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX]) {
     const f2x HALF = pk2(0.5f, 0.5f);
-#pragma unroll 2
+#pragma unroll 4
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
         const ulonglong2 WC = *reinterpret_cast<const ulonglong2*>(&cs[c].w);   // (w, w), (kappa c2, kappa c2)
