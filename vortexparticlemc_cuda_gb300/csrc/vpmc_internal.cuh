@@ -269,6 +269,22 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 // Warp-wide compensated reduction of (s, c) pairs (fixed tree); all lanes get it.
+// The same over aligned groups of G lanes (G a power of two <= 32); every lane
+// of the warp must take part.
+template <int G>
+__device__ __forceinline__ float group_sum_comp(float s, float c) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        float t, e;
+        const bool lo = (threadIdx.x & o) == 0;
+        two_sum(lo ? s : s2, lo ? s2 : s, t, e);
+        c = (lo ? c + c2 : c2 + c) - e;
+        s = t;
+    }
+    return s - c;
+}
 __device__ __forceinline__ float warp_sum_comp(float s, float c) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

@@ -163,13 +163,21 @@ __device__ __forceinline__ float2 aux_point(float2 x, int a, float dx) {
 
 __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
     const int Q = a.N1 + a.naux * a.N2;
-    const long total = a.nt * 2 * Q;
+    const uint32_t Q2 = uint32_t(2 * Q);
+    const uint32_t total = uint32_t(a.nt) * Q2;   // samples of one chunk (< 2^31)
     const unsigned long long step = *a.step;
-    for (long sid = long(blockIdx.x) * blockDim.x + threadIdx.x; sid < total; sid += long(gridDim.x) * blockDim.x) {
-        const long tl = sid / (2 * Q);
-        const int rem = int(sid - tl * 2 * Q);
-        const int s = rem / Q, j = rem - s * Q;
-        const long t = a.t0 + tl;
+    // sample sid = (target tl, sign s, sample j): decomposed once, then advanced
+    // by the grid stride without dividing again
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t dtl = stride / Q2, drem = stride - dtl * Q2;
+    uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t tl = sid / Q2, rem = sid - tl * Q2;
+    for (; sid < total; sid += stride) {
+        const int s = rem >= uint32_t(Q) ? 1 : 0, j = int(rem) - s * Q;
+        const long t = a.t0 + long(tl);
+        tl += dtl;
+        rem += drem;
+        if (rem >= Q2) { rem -= Q2; ++tl; }
         const int ii = inst_of(a.mc, a.n_inst, t);
         const InstMC& I = a.mc[ii];
         const GridInst& G = a.gi[ii];
@@ -218,7 +226,7 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
                     rr = (jt.x * (1.f - tt) + jt.y * tt) * I.hw;
                 }
                 float sn, cs;
-                sincosf(2.f * kPiF * u01(r.w), &sn, &cs);
+                sincospif(2.f * u01(r.w), &sn, &cs);   // angle 2 pi u
                 const float jx = rr * cs, jy = rr * sn;
                 if (a.F) {
                     // mul_mat2(F, r) (include/monte_carlo_bs.cuh:99-103)
@@ -234,11 +242,10 @@ __global__ void __launch_bounds__(256) k_gen(GenArgs a) {
             const int ax = a.naux > 1 ? (j - a.N1) / a.N2 : 0;
             const float2 xa = aux_point(x, ax, I.dx);
             const float R = disk_radius(xa, I.periodic != 0, I.Lx, I.Ly);
-            const float phi = 2.f * kPiF * u01(r.x);
             const float ur = u01(r.y);
             const float rr = I.law == VPMC_LAW_REFERENCE ? R * sqrtf(ur) : R * ur;
             float sn, cs;
-            sincosf(phi, &sn, &cs);
+            sincospif(2.f * u01(r.x), &sn, &cs);   // angle 2 pi u
             y.x = xa.x + rr * cs;
             y.y = xa.y + rr * sn;
         }
@@ -319,15 +326,23 @@ __device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f,
     return make_float2(-ry * sc, rx * sc);
 }
 
+// Plain method: 8 lanes per target, 4 targets per warp.  Each lane sums its
+// samples j = l, l + 8, ... (four loads in flight before their terms are
+// added), then the 8 lanes combine their compensated sums in a fixed tree.
+constexpr int kAccLanes = 8;
 __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, sub = lane & (kAccLanes - 1), grp = lane / kAccLanes;
+    constexpr int kPerWarp = 32 / kAccLanes;
     const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
     const int Q = a.N1 + a.N2;
     const float w1 = float(a.N1) / float(Q), w2 = float(a.N2) / float(Q);
     const float inv = 1.f / float(Q);
-    for (long tl = warp; tl < a.nt; tl += nwarps) {
-        const long t = a.t0 + tl;
+    // the loop runs the same trips in every lane of a warp (the group sums shuffle)
+    for (long tw = warp * kPerWarp; tw < a.nt; tw += nwarps * kPerWarp) {
+        const long tl = tw + grp;
+        const bool live = tl < a.nt;
+        const long t = a.t0 + (live ? tl : tw);
         const InstMC& I = a.mc[inst_of(a.mc, a.n_inst, t)];
         const float2 x = a.pos[t];
         const float R = disk_radius(x, I.periodic != 0, I.Lx, I.Ly);
@@ -336,29 +351,27 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
         for (int s = 0; s < 2; ++s) {
             KSum sx, sy;
             const long base = (tl * 2 + s) * Q;
-            // four samples per lane in flight before their terms are summed (in
-            // the order j = lane, lane + 32, ...)
-            for (int j0 = lane; j0 < Q; j0 += 128) {
+            for (int j0 = sub; j0 < Q; j0 += 4 * kAccLanes) {
                 float2 y[4];
                 float f[4];
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
-                    const int j = j0 + 32 * v;
-                    y[v] = j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
-                    f[v] = j < Q ? a.fv[base + j] : 0.f;
+                    const int j = j0 + kAccLanes * v;
+                    y[v] = live && j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
+                    f[v] = live && j < Q ? a.fv[base + j] : 0.f;
                 }
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
-                    if (j0 + 32 * v >= Q) break;
+                    if (j0 + kAccLanes * v >= Q) break;
                     const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
                     sx.add(c.x);
                     sy.add(c.y);
                 }
             }
-            u[s][0] = warp_sum_comp(sx.s, sx.c) * inv;
-            u[s][1] = warp_sum_comp(sy.s, sy.c) * inv;
+            u[s][0] = group_sum_comp<kAccLanes>(sx.s, sx.c) * inv;
+            u[s][1] = group_sum_comp<kAccLanes>(sy.s, sy.c) * inv;
         }
-        if (lane == 0) {
+        if (live && sub == 0) {
             const float vx = u[0][0] - u[1][0], vy = u[0][1] - u[1][1];
             a.vel[t] = make_float2(vx, vy);
             if (a.advect) {
@@ -842,7 +855,7 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         } else {
             AccArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, s->fv, t0, nt, s->N1, s->N2, advect ? 1 : 0, s->vel,
                        s->pos_next};
-            VPMC_LAUNCH(k_accum, blocks_for(nt * 32), 256, 0, st, aa);
+            VPMC_LAUNCH(k_accum, blocks_for(nt * kAccLanes), 256, 0, st, aa);
         }
     }
     if (advect) {
@@ -1276,7 +1289,7 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
         }
     }
     cudaStream_t st = s->ctx->stream;
-    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {2, 8}, {3, 8}, {4, 8}};
+    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
     struct Trial { int k, q; float ms; double check; };
     std::vector<Trial> tr;
     for (const auto& c : cands) {
