@@ -42,6 +42,9 @@ METRIC = "particle-steps/s at fixed vel. RMS err vs FP64 direct sum; % HBM roofl
 WORKLOADS = {
     "tg2048": dict(Nx=2048, hwr=16.0, N1=64, N2=64, dt=2.5e-4),
     "tg512": dict(Nx=512, hwr=16.0, N1=32, N2=32, dt=5e-4),
+    # tg2048's samples per target (and so its queries per bin) on a 512^2 lattice: a
+    # profiling-sized stand-in for the bench workload
+    "tg512s": dict(Nx=512, hwr=16.0, N1=64, N2=64, dt=5e-4),
     "tg256": dict(Nx=256, hwr=8.0, N1=32, N2=32, dt=1e-3),
     "tg64": dict(Nx=64, hwr=4.0, N1=16, N2=16, dt=1e-3),
     # 64 periodic instances, Nx from {96..384}, 8 Gaussian vortices each, one graph per step

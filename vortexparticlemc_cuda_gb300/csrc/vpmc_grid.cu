@@ -287,16 +287,27 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_coarse(const float2* 
     extern __shared__ __align__(16) uint4 srec[];   // kTileRecs
     __shared__ uint32_t hist[kTargetSuper], loff[kTargetSuper], s_warp[32];
     __shared__ long long goff[kTargetSuper];
-    for (long t0 = long(blockIdx.x) * kTileRecs; t0 < M; t0 += long(gridDim.x) * kTileRecs) {
-        for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) hist[k] = 0u;
-        __syncthreads();
-        uint32_t bb[kPlaceTile], lr[kPlaceTile];
+    // the tile's bins and points are loaded one tile ahead (while the previous
+    // tile is written out)
+    uint32_t bb[kPlaceTile], lr[kPlaceTile];
+    float2 pp[kPlaceTile];
+    auto load_tile = [&](long t) {
 #pragma unroll
         for (int j = 0; j < kPlaceTile; ++j) {
-            const long m = t0 + long(j) * kPlaceThreads + threadIdx.x;
+            const long m = t + long(j) * kPlaceThreads + threadIdx.x;
             bb[j] = m < M ? qbin[m] : kNoBin;
-            if (bb[j] != kNoBin) lr[j] = atomicAdd(&hist[bb[j] >> shift], 1u);
+            pp[j] = m < M ? pts[m] : make_float2(0.f, 0.f);   // unwrapped: pass 3 wraps it
         }
+    };
+    long t0 = long(blockIdx.x) * kTileRecs;
+    if (t0 >= M) return;
+    load_tile(t0);
+    for (;;) {
+        for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) hist[k] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kPlaceTile; ++j)
+            if (bb[j] != kNoBin) lr[j] = atomicAdd(&hist[bb[j] >> shift], 1u);
         __syncthreads();
         for (int k = threadIdx.x; k < nsuper; k += kPlaceThreads) loff[k] = hist[k];
         __syncthreads();
@@ -309,16 +320,19 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_coarse(const float2* 
         for (int j = 0; j < kPlaceTile; ++j) {
             if (bb[j] == kNoBin) continue;
             const long m = t0 + long(j) * kPlaceThreads + threadIdx.x;
-            const float2 p = pts[m];   // unwrapped: pass 3 wraps it and derives the image flags
-            srec[loff[bb[j] >> shift] + lr[j]] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y),
+            srec[loff[bb[j] >> shift] + lr[j]] = make_uint4(__float_as_uint(pp[j].x), __float_as_uint(pp[j].y),
                                                             uint32_t(m), bb[j]);
         }
         __syncthreads();
+        const long tn = t0 + long(gridDim.x) * kTileRecs;
+        if (tn < M) load_tile(tn);
         for (uint32_t i = threadIdx.x; i < ntile; i += kPlaceThreads) {
             const uint4 r = srec[i];
             tmp[goff[r.w >> shift] + i] = r;
         }
         __syncthreads();
+        if (tn >= M) break;
+        t0 = tn;
     }
 }
 
@@ -362,21 +376,30 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_window(const uint4* _
     __shared__ long long goff[kWinMax];
     __shared__ uint32_t s_lo, s_hi;
     const long n = min(long(*total), M);
-    for (long t0 = long(blockIdx.x) * kTileRecs; t0 < n; t0 += long(gridDim.x) * kTileRecs) {
-        if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
-        __syncthreads();
-        uint4 r[kPlaceTile];
-        uint32_t lo = 0xffffffffu, hi = 0u;
+    // records loaded one tile ahead (while the previous tile is written out)
+    uint4 r[kPlaceTile];
+    auto load_tile = [&](long t) {
 #pragma unroll
         for (int j = 0; j < kPlaceTile; ++j) {
-            const long i = t0 + long(j) * kPlaceThreads + threadIdx.x;
+            const long i = t + long(j) * kPlaceThreads + threadIdx.x;
             r[j] = i < n ? tmp[i] : make_uint4(0u, 0u, 0u, kNoBin);
-            if (r[j].w != kNoBin) { lo = min(lo, r[j].w >> wshift); hi = max(hi, r[j].w >> wshift); }
         }
+    };
+    long t0 = long(blockIdx.x) * kTileRecs;
+    if (t0 >= n) return;
+    if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
+    load_tile(t0);
+    __syncthreads();
+    for (;;) {
+        uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int j = 0; j < kPlaceTile; ++j)
+            if (r[j].w != kNoBin) { lo = min(lo, r[j].w >> wshift); hi = max(hi, r[j].w >> wshift); }
         atomicMin(&s_lo, lo);
         atomicMax(&s_hi, hi);
         __syncthreads();
         const uint32_t wlo = s_lo, span = s_hi >= s_lo ? s_hi - s_lo + 1u : 0u;
+        const long tn = t0 + long(gridDim.x) * kTileRecs;
         if (span > uint32_t(kWinMax)) {
 #pragma unroll
             for (int j = 0; j < kPlaceTile; ++j) {
@@ -385,6 +408,11 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_window(const uint4* _
                 tmp2[qstart[w << wshift] + atomicAdd(&win_fill[w], 1u)] = r[j];
             }
             __syncthreads();
+            if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
+            if (tn < n) load_tile(tn);
+            __syncthreads();
+            if (tn >= n) break;
+            t0 = tn;
             continue;
         }
         for (uint32_t k = threadIdx.x; k < span; k += kPlaceThreads) hist[k] = 0u;
@@ -405,11 +433,15 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_window(const uint4* _
         for (int j = 0; j < kPlaceTile; ++j)
             if (r[j].w != kNoBin) srec[loff[(r[j].w >> wshift) - wlo] + lr[j]] = r[j];
         __syncthreads();
+        if (threadIdx.x == 0) { s_lo = 0xffffffffu; s_hi = 0u; }
+        if (tn < n) load_tile(tn);
         for (uint32_t i = threadIdx.x; i < ntile; i += kPlaceThreads) {
             const uint4 q = srec[i];
             tmp2[goff[(q.w >> wshift) - wlo] + i] = q;
         }
         __syncthreads();
+        if (tn >= n) break;
+        t0 = tn;
     }
 }
 
@@ -427,20 +459,24 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
     __shared__ uint32_t sub[kSubCells * kWinBinsMax];   // per (sub-cell, bin of the window): count, then first slot
     __shared__ float4 corg[kWinBinsMax];                 // per bin of the window: its cell, for subcell_key
     const long nwin = ((nbins - 1) >> wshift) + 1;
-    for (long w = blockIdx.x; w < nwin; w += gridDim.x) {
-        const long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
-        const uint32_t start = qstart[b0], nw = qstart[b1] - start;
-        const bool fits = nw <= uint32_t(kWinCap);
-        // the window's records are loaded together with its bin starts (one
-        // round trip), then slotted
-        uint4 r[kPer];
-        if (fits) {
+    long w = blockIdx.x;
+    if (w >= nwin) return;
+    // window w's bounds and (when it fits) its records: loaded one window ahead,
+    // so the loads overlap the previous window's write-out
+    long b0 = w << wshift, b1 = min(nbins, b0 + (1L << wshift));
+    uint32_t start = qstart[b0], nw = qstart[b1] - start;
+    uint4 r[kPer];
+    auto load_records = [&](uint32_t st, uint32_t n) {
+        if (n > uint32_t(kWinCap)) return;
 #pragma unroll
-            for (int j = 0; j < kPer; ++j) {
-                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
-                r[j] = k < nw ? tmp2[start + k] : make_uint4(0u, 0u, 0u, 0u);
-            }
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+            r[j] = k < n ? tmp2[st + k] : make_uint4(0u, 0u, 0u, 0u);
         }
+    };
+    load_records(start, nw);
+    for (;;) {
+        const bool fits = nw <= uint32_t(kWinCap);
         const uint32_t nb = uint32_t(b1 - b0);
         for (long b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
             cnt[b - b0] = qstart[b];
@@ -490,9 +526,26 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
             }
         }
         __syncthreads();
+        // the next window's bounds and records go out before this one is written
+        const long wn = w + gridDim.x;
+        long nb0 = 0, nb1 = 0;
+        uint32_t nstart = 0, nnw = 0;
+        if (wn < nwin) {
+            nb0 = wn << wshift;
+            nb1 = min(nbins, nb0 + (1L << wshift));
+            nstart = qstart[nb0];
+            nnw = qstart[nb1] - nstart;
+            load_records(nstart, nnw);
+        }
         if (fits)
             for (uint32_t k = threadIdx.x; k < nw; k += blockDim.x) qrec[start + k] = buf[k];
         __syncthreads();
+        if (wn >= nwin) break;
+        w = wn;
+        b0 = nb0;
+        b1 = nb1;
+        start = nstart;
+        nw = nnw;
     }
 }
 
