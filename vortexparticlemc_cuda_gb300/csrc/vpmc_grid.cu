@@ -234,9 +234,10 @@ __global__ void k_scatter_ranked(const float2* __restrict__ pts, long M, const G
 constexpr int kPlaceThreads = 512;
 constexpr int kPlaceTile = 8;                                // records per thread per tile
 constexpr int kTileRecs = kPlaceThreads * kPlaceTile;        // 4096 records = 64 KB staged per tile
-constexpr int kTargetSuper = 256;                            // super-bins per grid
+constexpr int kTargetSuper = 512;                            // super-bins per grid
 constexpr int kWinMax = 2048;                                // windows one tile may sort in shared memory
-constexpr int kWinCap = 8192;                                // records a window assembles in shared memory
+constexpr int kWinCap = 4096;                                // records a window assembles in shared memory
+constexpr int kAsmThreads = 512;                             // window assembly: 2 CTAs per SM
 constexpr int kWinBinsMax = 256;                             // bins per window at most
 
 // Exclusive prefix sum of v[0..n) in place (shared memory, n small), block
@@ -449,11 +450,11 @@ __global__ void __launch_bounds__(kPlaceThreads) k_scatter_window(const uint4* _
 // counters started at qstart of its bin, the window is built in shared memory
 // and written out as one contiguous block (an over-full window stores
 // directly).
-__global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restrict__ tmp2, long nbins, int wshift,
+__global__ void __launch_bounds__(kAsmThreads, 2) k_scatter_assemble(const uint4* __restrict__ tmp2, long nbins, int wshift,
                                                             const uint32_t* __restrict__ qstart,
                                                             const GridInst* __restrict__ inst, int n_inst,
                                                             QRec* __restrict__ qrec) {
-    constexpr int kPer = kWinCap / 1024;            // records per thread of a window that fits
+    constexpr int kPer = kWinCap / kAsmThreads;     // records per thread of a window that fits
     extern __shared__ __align__(16) QRec buf[];   // kWinCap records
     __shared__ uint32_t cnt[kWinBinsMax];
     __shared__ uint32_t sub[kSubCells * kWinBinsMax];   // per (sub-cell, bin of the window): count, then first slot
@@ -470,7 +471,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
         if (n > uint32_t(kWinCap)) return;
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
-            const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+            const uint32_t k = threadIdx.x + uint32_t(j) * uint32_t(kAsmThreads);
             r[j] = k < n ? tmp2[st + k] : make_uint4(0u, 0u, 0u, 0u);
         }
     };
@@ -492,7 +493,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
             uint32_t kr[kPer];   // bin in the window | sub-cell << 8 | rank within (sub-cell, bin) << 12
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
-                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+                const uint32_t k = threadIdx.x + uint32_t(j) * uint32_t(kAsmThreads);
                 if (k >= nw) break;
                 const uint32_t bl = r[j].w - uint32_t(b0);
                 const QRec q = make_qrec(r[j], inst, n_inst);
@@ -513,7 +514,7 @@ __global__ void __launch_bounds__(1024) k_scatter_assemble(const uint4* __restri
             __syncthreads();
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
-                const uint32_t k = threadIdx.x + uint32_t(j) * 1024u;
+                const uint32_t k = threadIdx.x + uint32_t(j) * uint32_t(kAsmThreads);
                 if (k >= nw) break;
                 const uint32_t slot = sub[((kr[j] >> 8) & 15u) * nb + (kr[j] & 255u)] + (kr[j] >> 12);
                 buf[slot - start] = QRec{__uint_as_float(r[j].x), __uint_as_float(r[j].y), r[j].z, r[j].w};
@@ -1562,7 +1563,7 @@ int scatter_ranked(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const flo
                     q.super_fill, q.tmp);
         VPMC_LAUNCH(k_scatter_window, tgrid, kPlaceThreads, tile_smem, st, q.tmp, q.qstart + g.nbins, M, wshift,
                     q.qstart, q.win_fill, q.tmp2);
-        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, ctx->sm_count))), 1024, win_smem,
+        VPMC_LAUNCH(k_scatter_assemble, int(std::max<long>(1, std::min<long>(nwin, 2L * ctx->sm_count))), kAsmThreads, win_smem,
                     st, q.tmp2, g.nbins, wshift, q.qstart, g.inst, g.n_inst, q.qrec);
         return VPMC_OK;
     }
