@@ -11,10 +11,10 @@ namespace vpmc {
 
 namespace {
 
-constexpr int kEvalThreads = 128;
+constexpr int kEvalThreads = 32;
 constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
-constexpr int kCandCap = 768;                  // candidates staged per batch (24 KB: 8 CTAs per SM)
+constexpr int kCandCap = 200;                  // candidates staged per batch (6.25 KB: 24 one-warp CTAs per SM)
 constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
@@ -718,12 +718,13 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
     }
 }
 
-// The packed FP32 kernels keep to 64 registers with 4 queries per thread (eight
-// CTAs of 128 threads per SM: their 24 KB staging buffers fit eight times in
-// shared memory) and to 128 with 8 (four CTAs per SM).
+// The packed FP32 kernels run one-warp CTAs, 24 per SM (their 6.25 KB staging
+// buffers fit 24 times in shared memory; 85 registers a thread at most) with 4
+// queries per thread, 12 per SM with 8.  One warp per CTA: no warp of an item
+// waits at a barrier for another.
 constexpr int eval_min_blocks(int mode, int qpt) {
     return (mode == EVAL_FIELD || mode == EVAL_FIELD9 || mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F)
-               ? (qpt == 4 ? 8 : 4) : 1;
+               ? (qpt == 4 ? 24 : 12) : 1;
 }
 
 template <int MODE, int QPT>
