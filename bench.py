@@ -168,11 +168,14 @@ def cpu_reference_sample(wl, pos, omega, budget_s, seed=17, nthreads=0, fixed_ta
         st = O.OracleState(pos, omega, prm)
     rng = np.random.default_rng(seed)
     if fixed_targets is None:
-        t_probe = pos[rng.choice(len(pos), 16, replace=False)]
+        # a probe large enough to keep every host thread busy sizes the sample
+        # to about budget_s seconds
+        n_probe = min(len(pos), 512)
+        t_probe = pos[rng.choice(len(pos), n_probe, replace=False)]
         t0 = time.perf_counter()
         _, nt = O.mc_velocity_omp(st, t_probe, prm.N1, prm.N2, seed, nthreads)
         dt = time.perf_counter() - t0
-        m = int(np.clip(16 * budget_s / max(dt, 1e-6), 16, 200000))
+        m = int(np.clip(n_probe * budget_s / max(dt, 1e-6), 16, 400000))
     else:
         m = fixed_targets
     targets = pos[rng.choice(len(pos), m, replace=m > len(pos))]
