@@ -947,6 +947,9 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
             }
             if ((tid & 31) == 0) s_wb[tid >> 5] = make_float4(bx0 - s_ox, bx1 - s_ox, by0 - s_oy, by1 - s_oy);
+            // the warp's lanes read the box below, possibly before any CTA barrier
+            // (a first batch issued with the walk skips the planning barrier)
+            __syncwarp();
         }
 
         for (;;) {
