@@ -146,7 +146,7 @@ def test_step_host_roundtrip(cuda):
 def test_tuning_does_not_change_results_beyond_rounding(cuda):
     sim, pos, om, prm = _setup(cuda, law=1)
     base = sim.velocity(step=1).cpu().numpy()
-    for k, q in ((1, 4), (3, 8), (2, 8), (4, 4)):
+    for k, q in ((1, 4), (3, 8), (2, 8), (4, 4), (3, 6), (2, 6)):
         sim.set_tuning(k, q)
         v = sim.velocity(step=1).cpu().numpy()
         assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max(), (k, q)
@@ -156,7 +156,7 @@ def test_autotune_picks_a_candidate_and_caches(cuda):
     sim, pos, om, prm = _setup(cuda, law=1)
     base = sim.velocity(step=2).cpu().numpy()
     k, q, ms = sim.autotune()
-    assert k in (2, 3, 4) and q in (4, 8) and ms > 0
+    assert k in (2, 3, 4) and q in (4, 6, 8) and ms > 0
     assert sim.tuning() == (k, q)
     v = sim.velocity(step=2).cpu().numpy()
     assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max()

@@ -720,11 +720,11 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
 
 // The packed FP32 kernels run one-warp CTAs, 24 per SM (their 6.25 KB staging
 // buffers fit 24 times in shared memory; 85 registers a thread at most) with 4
-// queries per thread, 12 per SM with 8.  One warp per CTA: no warp of an item
+// queries per thread, 16 per SM with 6 and 12 with 8.  One warp per CTA: no warp of an item
 // waits at a barrier for another.
 constexpr int eval_min_blocks(int mode, int qpt) {
     return (mode == EVAL_FIELD || mode == EVAL_FIELD9 || mode == EVAL_FIELD_F || mode == EVAL_FIELD9_F)
-               ? (qpt == 4 ? 24 : 12) : 1;
+               ? (qpt == 4 ? 24 : qpt == 6 ? 16 : 12) : 1;
 }
 
 template <int MODE, int QPT>
@@ -1385,7 +1385,7 @@ int blocks_for(long n, int threads = 256) {
 
 int default_k() { return 2; }
 
-int query_chunk(int qpt) { return (qpt == 8 ? 8 : 4) * kEvalThreads; }
+int query_chunk(int qpt) { return (qpt == 8 ? 8 : qpt == 6 ? 6 : 4) * kEvalThreads; }
 
 long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     if (k <= 0) k = default_k();
@@ -1590,9 +1590,11 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
     switch (L.mode) {
         case EVAL_FIELD:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);
+            if (L.qpt == 6) return launch_eval_t<EVAL_FIELD, 6>(ctx, a);
             return launch_eval_t<EVAL_FIELD, 4>(ctx, a);
         case EVAL_FIELD9:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD9, 8>(ctx, a);
+            if (L.qpt == 6) return launch_eval_t<EVAL_FIELD9, 6>(ctx, a);
             return launch_eval_t<EVAL_FIELD9, 4>(ctx, a);
         case EVAL_FIELD_EXC:
             if (L.qpt != 4) return VPMC_ERR_INVALID;
@@ -1605,9 +1607,11 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
             return launch_eval_t<EVAL_SPMV32, 4>(ctx, a);
         case EVAL_FIELD_F:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD_F, 8>(ctx, a);
+            if (L.qpt == 6) return launch_eval_t<EVAL_FIELD_F, 6>(ctx, a);
             return launch_eval_t<EVAL_FIELD_F, 4>(ctx, a);
         case EVAL_FIELD9_F:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD9_F, 8>(ctx, a);
+            if (L.qpt == 6) return launch_eval_t<EVAL_FIELD9_F, 6>(ctx, a);
             return launch_eval_t<EVAL_FIELD9_F, 4>(ctx, a);
         case EVAL_FIELD_F_EXC:
             if (L.qpt != 4) return VPMC_ERR_INVALID;

@@ -1253,7 +1253,7 @@ int vpmc_sim_set_precision(vpmc_sim* s, int bits) {
 }
 
 int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
-    if (!s || k_walk < 0 || k_walk > 8 || !(qpt == 0 || qpt == 4 || qpt == 8)) return VPMC_ERR_INVALID;
+    if (!s || k_walk < 0 || k_walk > 8 || !(qpt == 0 || qpt == 4 || qpt == 6 || qpt == 8)) return VPMC_ERR_INVALID;
     s->k_walk = k_walk;
     s->qpt = qpt == 0 ? 4 : qpt;
     VPMC_TRY(alloc_work(s));
@@ -1289,7 +1289,7 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
         }
     }
     cudaStream_t st = s->ctx->stream;
-    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
+    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {3, 6}, {4, 6}, {6, 6}, {8, 6}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
     struct Trial { int k, q; float ms; double check; };
     std::vector<Trial> tr;
     for (const auto& c : cands) {
