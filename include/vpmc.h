@@ -376,7 +376,7 @@ int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
 int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
 
 /* Autotuner (no reference counterpart): times one full MIS velocity pass per
- * candidate (k_walk, queries_per_thread) in {2,3,4,6,8}x{4,8} + {3,4,6,8}x{6}, keeps
+ * candidate (k_walk, queries_per_thread) in {2..8}x{4} + {3,4,6,8}x{6} + {2,3,4,6,8}x{8}, keeps
  * the fastest, and caches the choice in-process by (hwr, samples per target,
  * particles per h_w^2).  Results do not depend on the choice beyond FP32
  * rounding of the field sums, and the autotuner checks that: each

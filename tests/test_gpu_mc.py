@@ -156,7 +156,7 @@ def test_autotune_picks_a_candidate_and_caches(cuda):
     sim, pos, om, prm = _setup(cuda, law=1)
     base = sim.velocity(step=2).cpu().numpy()
     k, q, ms = sim.autotune()
-    assert k in (2, 3, 4) and q in (4, 6, 8) and ms > 0
+    assert 2 <= k <= 8 and q in (4, 6, 8) and ms > 0
     assert sim.tuning() == (k, q)
     v = sim.velocity(step=2).cpu().numpy()
     assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max()

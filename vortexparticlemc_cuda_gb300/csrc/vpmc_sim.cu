@@ -1289,7 +1289,8 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
         }
     }
     cudaStream_t st = s->ctx->stream;
-    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {6, 4}, {8, 4}, {3, 6}, {4, 6}, {6, 6}, {8, 6}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
+    const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {5, 4}, {6, 4}, {7, 4}, {8, 4}, {3, 6}, {4, 6}, {6, 6},
+                            {8, 6}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
     struct Trial { int k, q; float ms; double check; };
     std::vector<Trial> tr;
     for (const auto& c : cands) {
