@@ -156,6 +156,54 @@ def profile_traffic(workload: str):
 
 
 # ------------------------------------------------------------------ CPU side
+def in_support_pairs(sim, sps, counts, n_targets=128, seed=5):
+    """Mean number of in-support pairs per sample query: over every sample of
+    `n_targets` random targets of the last MIS pass's last chunk, the particles
+    of the sample's sign subset within h_w of the (wrapped) sample point; a
+    sample the unbiased law drops (more than two periods out) or that leaves a
+    non-periodic domain counts 0.  Call right after a non-advecting pass, so the
+    particles are where the pass drew the samples."""
+    from scipy.spatial import cKDTree
+    from vortexparticlemc_cuda_gb300.phash import LAW_UNBIASED
+    pos_d, om_d, _ = sim.particles()
+    pos, om = pos_d.cpu().numpy().astype(np.float64), om_d.cpu().numpy()
+    geo = sim.geometry()
+    q2 = geo["samples_per_target"]
+    t0, _ = sim.read_samples(0, 0)
+    nt = geo["N"] - t0
+    begins = np.concatenate([[0], np.cumsum(counts)])
+    trees = {}
+    tot, nq = 0, 0
+    for tl in np.random.default_rng(seed).choice(nt, size=min(n_targets, nt), replace=False):
+        t = t0 + int(tl)
+        i = int(np.searchsorted(begins, t, side="right") - 1)
+        sp = sps[i]
+        L = np.array([sp.Lx, sp.Ly])
+        if i not in trees:
+            p, w = pos[begins[i]:begins[i + 1]], om[begins[i]:begins[i + 1]]
+            if sp.periodic:
+                p = np.mod(p, L)
+                p = np.where(p >= L, p - L, p)
+            trees[i] = [cKDTree(p[sel], boxsize=L if sp.periodic else None) if sel.any() else None
+                        for sel in (w > 0, w < 0)]
+        _, y = sim.read_samples(int(tl) * q2, q2)
+        y = y.astype(np.float64)
+        for sgn in (0, 1):
+            ys = y[sgn * (q2 // 2):(sgn + 1) * (q2 // 2)]
+            nq += len(ys)
+            if sp.periodic:
+                k = np.floor(ys / L)
+                keep = np.all(np.abs(k) <= 2, 1) if sp.law == LAW_UNBIASED else np.ones(len(ys), bool)
+                ys = ys - k * L
+                ys = np.where(ys >= L, ys - L, ys)
+            else:
+                keep = np.all((ys >= 0) & (ys <= L), 1)
+            tree = trees[i][sgn]
+            if tree is not None and keep.any():
+                tot += int(np.sum(tree.query_ball_point(ys[keep], r=sp.h_w, return_length=True)))
+    return tot / max(nq, 1)
+
+
 def cpu_reference_sample(wl, pos, omega, budget_s, seed=17, nthreads=0, fixed_targets=None, st=None):
     """Time the reference CPU estimator (oracle restatement of
     monte_carlo_bs_cpu, pinned bit-exact to the reference sources) on a
@@ -349,6 +397,11 @@ def run_gpu(args, wl):
     ms = e0.elapsed_time(e1)
     log(f"timed {args.steps} steps: {ms / args.steps:.1f} ms/step, eval {np.mean(eval_ms):.1f} ms/step")
     stats = sim.last_stats()
+    # in-support pairs per sample query, counted on the samples of one more
+    # (non-advecting) pass: the algorithmic work of the evaluation
+    sim.velocity()
+    n_hit = in_support_pairs(sim, sps, counts)
+    log(f"in-support pairs per sample query: {n_hit:.1f}")
     ms = max_over_ranks(ms, dev)
     value = replica_throughput(N, world, args.steps, ms)
 
@@ -374,7 +427,6 @@ def run_gpu(args, wl):
     # roofline of the dominant kernel (field evaluation, FP32-pipe bound)
     peaks, peak_kind = measured_peaks()
     Q = 2 * (wl["N1"] + (5 if args.deform else 1) * wl["N2"])
-    n_hit = np.pi * wl["hwr"] ** 2 / 2.0            # same-sign particles within h_w (TG: half of them)
     launches = max(1, geo["chunks"])
     eval_ms_launch = float(np.mean(eval_ms)) / launches
     samples_launch = N * Q / launches
@@ -389,7 +441,10 @@ def run_gpu(args, wl):
             "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
                            f"({peak_kind}); the kernel is FP32-pipe bound: no tensor-core or HBM bound applies",
             "traffic": None if args.deform else profile_traffic(args.workload),
-            "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.0f} in-support pairs x 16 flop",
+            "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.1f} in-support pairs x 16 flop",
+            "in_support_pairs": ("same-sign particles within h_w of the wrapped sample point (" +
+                                 ("isotropic radius, " if args.deform else "") +
+                                 "mean over all samples of 128 random targets of a pass; dropped samples count 0)"),
             "eval_ms_per_launch": eval_ms_launch, "eval_share_of_step": float(np.mean(eval_ms)) / (ms / args.steps)}
     if clocks.get("sm_mhz"):
         roof["frac_at_sampled_clock"] = achieved / (sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)

@@ -397,6 +397,18 @@ int vpmc_sim_last_stats(vpmc_sim* sim, int* launches_per_step, float* eval_ms);
  * eval launches in the last timed step}.  No reference counterpart. */
 int vpmc_sim_geometry(vpmc_sim* sim, long long* info);
 
+/* Sample points of the last chunk drawn by the last MIS pass (a step, a
+ * velocity pass or an autotuner pass): count (x, y) pairs from sample index
+ * `first` into the HOST array xy, where sample (t - t0) * samples_per_target
+ * + sign * samples_per_target / 2 + j is sample j of target t and the given
+ * sign (0: positive strengths, 1: negative); *t0 (may be NULL) receives the
+ * chunk's first target.  Points are as drawn (before the periodic wrap).
+ * VPMC_ERR_INVALID when no pass has drawn samples since the working set was
+ * last (re)allocated or reused, or when the range leaves the chunk.  No
+ * reference counterpart (instrumentation: the in-support pair count of the
+ * evaluation's roofline). */
+int vpmc_sim_read_samples(vpmc_sim* sim, long long first, long long count, long long* t0, float* xy);
+
 /* ---------------------------------------------------------------- misc */
 /* Philox4x32-10 (Salmon et al., SC'11) block function, host evaluation:
  * out[4] = philox(ctr[4], key[2]).  Exposed for known-answer tests. */

@@ -87,3 +87,41 @@ def test_context_closed_before_its_simulation(cuda):
     sim.step(1)
     assert np.isfinite(sim.particles()[0].cpu().numpy()).all()
     sim.close()                       # the last holder frees the context
+
+
+def test_sample_readback(cuda):
+    """vpmc_sim_read_samples: refused before any pass and outside the chunk;
+    after a non-advecting pass the disk samples of a target lie within the
+    sampling-disk radius of it, and every branch-1 sample lies within h_w of a
+    particle of its sign subset (periodic distance)."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    pos = O.lattice(32)
+    om = (O.taylor_green(pos) * np.float32(1e-3)).astype(np.float32)
+    prm = P.SimParam(dt=1e-3, Nx=32, hwr=4, N1=8, N2=8, law=P.LAW_UNBIASED, seed=3)
+    sim = P.Simulation(prm, [len(pos)])
+    sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+    sim.prepare()
+    with pytest.raises(P.VpmcError):
+        sim.read_samples(0, 1)
+    sim.velocity(step=0)
+    q2 = sim.geometry()["samples_per_target"]
+    assert q2 == 2 * (prm.N1 + prm.N2)
+    t0, none = sim.read_samples(0, 0)
+    assert t0 == 0 and none.shape == (0, 2)
+    with pytest.raises(P.VpmcError):
+        sim.read_samples(len(pos) * q2 - 1, 2)
+    L = np.array([prm.Lx, prm.Ly])
+    R = float(np.hypot(prm.Lx, prm.Ly))
+    for t in (0, 17, len(pos) - 1):
+        _, y = sim.read_samples(t * q2, q2)
+        assert np.isfinite(y).all()
+        _, again = sim.read_samples(t * q2, q2)
+        assert np.array_equal(y, again)
+        for s, sel in ((0, om > 0), (1, om < 0)):
+            ys = y[s * (q2 // 2):(s + 1) * (q2 // 2)].astype(np.float64)
+            disk = ys[prm.N1:]
+            assert (np.linalg.norm(disk - pos[t], axis=1) <= R * (1 + 1e-6)).all()
+            d = ys[:prm.N1, None, :] - pos[sel][None, :, :].astype(np.float64)
+            d -= np.round(d / L) * L
+            nearest = np.sqrt((d ** 2).sum(-1)).min(1)
+            assert (nearest <= prm.h_w * (1 + 1e-5) + 1e-6).all()

@@ -96,6 +96,7 @@ SIGNATURES = {
     "vpmc_sim_autotune": (_i, [_vp, _vp, _vp, _vp]),
     "vpmc_sim_last_stats": (_i, [_vp, _vp, _vp]),
     "vpmc_sim_geometry": (_i, [_vp, _vp]),
+    "vpmc_sim_read_samples": (_i, [_vp, C.c_longlong, C.c_longlong, _vp, _vp]),
     "vpmc_philox4x32_10": (None, [_vp, _vp, _vp]),
 }
 

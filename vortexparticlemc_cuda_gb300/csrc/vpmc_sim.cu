@@ -754,6 +754,8 @@ int alloc_work(vpmc_sim* s) {
         carve_items(c, nb, ns, &s->it);
         carve_queries(c, nb, ns, &s->q, true);
         s->ys = c.take<float2>(size_t(ns));
+        s->ys_t0 = -1;
+        s->ys_nt = 0;
         s->fv = c.take<float>(size_t(ns));
         s->fv64 = s->precision == 64 ? c.take<double>(size_t(ns)) : nullptr;
         s->cum64 = c.take<double>(2 * size_t(s->n_inst));
@@ -800,6 +802,12 @@ int refresh_cover(vpmc_sim* s, bool from_step, bool reset, bool realloc = false)
     if (changed) s->cover = need;
     if (changed || realloc) VPMC_TRY(alloc_work(s));
     return VPMC_OK;
+}
+
+// The sample buffer holds the last chunk's samples after a pass.
+void mark_samples(vpmc_sim* s) {
+    s->ys_t0 = ((s->N - 1) / s->chunk_targets) * s->chunk_targets;
+    s->ys_nt = s->N - s->ys_t0;
 }
 
 // Issue one MIS pass over all targets (advect: positions -> pos_next, then
@@ -858,6 +866,7 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
             VPMC_LAUNCH(k_accum, blocks_for(nt * kAccLanes), 256, 0, st, aa);
         }
     }
+    mark_samples(s);
     if (advect) {
         VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
         if (def)
@@ -920,6 +929,7 @@ int sim::run_pass(vpmc_sim* s, bool advect, int use_graph) {
         if (advect) return VPMC_OK;   // the eager pass was this call's step
     }
     VPMC_CUDA(cudaGraphLaunch(*gx, st));
+    mark_samples(s);
     if (advect) s->step += 1;
     return VPMC_OK;
 }
@@ -1152,6 +1162,8 @@ int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, i
     if (!omega_field) {
         // reuse the sample-position scratch for the FP64 right-hand side
         b = reinterpret_cast<double*>(s->ys);
+        s->ys_t0 = -1;
+        s->ys_nt = 0;
         if (s->chunk_targets * 2L * (s->N1 + s->N2) < s->N) return VPMC_ERR_CAPACITY;
         VPMC_LAUNCH(k_taylor_green, blocks_for(s->N), 256, 0, st, s->pos, s->N, b);
     }
@@ -1347,6 +1359,18 @@ int vpmc_sim_last_stats(vpmc_sim* s, int* launches_per_step, float* eval_ms) {
     if (launches_per_step) *launches_per_step = s->launches_per_step;
     if (eval_ms) *eval_ms = s->eval_ms;
     return VPMC_OK;
+}
+
+int vpmc_sim_read_samples(vpmc_sim* s, long long first, long long count, long long* t0, float* xy) {
+    if (!s || first < 0 || count < 0 || (count > 0 && !xy)) return VPMC_ERR_INVALID;
+    if (s->ys_t0 < 0) return VPMC_ERR_INVALID;   // no pass has drawn samples into the current buffer
+    if (t0) *t0 = s->ys_t0;
+    if (first + count > s->ys_nt * 2LL * samples_per(s)) return VPMC_ERR_INVALID;
+    if (count == 0) return VPMC_OK;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    VPMC_CUDA(cudaMemcpyAsync(xy, s->ys + first, sizeof(float2) * size_t(count), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    return vpmc_context_sync(s->ctx);
 }
 
 int vpmc_sim_geometry(vpmc_sim* s, long long* info) {

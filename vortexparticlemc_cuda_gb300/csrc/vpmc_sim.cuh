@@ -121,6 +121,7 @@ struct vpmc_sim {
     ItemBufs it;
     QueryBufs q;
     float2* ys = nullptr;
+    long ys_t0 = -1, ys_nt = 0;        // targets whose samples ys holds (last chunk of the last pass)
     float* fv = nullptr;
     double* fv64 = nullptr;            // FP64 path only
     double* cum64 = nullptr;           // per instance Omega_+-, x9 when periodic (FP64 path)

@@ -395,6 +395,17 @@ class Simulation:
         keys = ("N", "chunk_targets", "chunks", "bins", "cells_x", "k_walk", "samples_per_target", "eval_launches")
         return dict(zip(keys, [int(v) for v in g]))
 
+    def read_samples(self, first: int, count: int):
+        """Sample points of the last chunk drawn by the last MIS pass (instrumentation):
+        (the chunk's first target, a (count, 2) float32 array of points as drawn).
+        Sample (t - t0) * samples_per_target + sign * samples_per_target // 2 + j
+        is sample j of target t for the positive (sign 0) or negative subset."""
+        xy = np.empty((int(count), 2), dtype=np.float32)
+        t0 = C.c_longlong()
+        check(lib().vpmc_sim_read_samples(self.h, int(first), int(count), C.byref(t0),
+                                          xy.ctypes.data_as(C.c_void_p)), "vpmc_sim_read_samples")
+        return t0.value, xy
+
     # adjoint (common random numbers, checkpoints every k steps)
     def record(self, nsteps: int, k_ckpt: int = 20):
         check(lib().vpmc_sim_record(self.h, int(nsteps), int(k_ckpt)), "vpmc_sim_record")
