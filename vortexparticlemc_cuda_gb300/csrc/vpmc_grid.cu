@@ -616,11 +616,6 @@ __device__ __forceinline__ f2x pk2(float a, float b) {
 __device__ __forceinline__ void up2(f2x v, float& a, float& b) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
-__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
-    f2x r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
 __device__ __forceinline__ f2x add2(f2x a, f2x b) {
     f2x r;
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));

@@ -45,11 +45,6 @@ __global__ void k_scatter_from_sorted(const double* __restrict__ xs, const uint3
         x[perm[p]] = float(xs[p]);
 }
 
-__global__ void k_f64_to_f32(const double* __restrict__ a, long n, float scale, float* __restrict__ b) {
-    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
-        b[i] = float(a[i]) * scale;
-}
-
 __global__ void k_scale_f32(float* __restrict__ a, long n, float s) {
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) a[i] *= s;
 }
