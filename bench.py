@@ -268,7 +268,8 @@ def run_reference(args, wl):
         # Fourier mode of the RBF matrix, so the first step already leaves only
         # FP32 rounding of b; the timed estimator does not depend on the rest
         omega, cg = strengths_cpu(wl, pos, b)
-    per_step_budget = max(1.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
+    per_step_budget = (args.ref_seconds if args.ref_seconds > 0
+                       else max(1.0, min(20.0, 90.0 / max(1, args.steps + args.warmup))))
     rate, nt, m, dt, st = cpu_reference_sample(wl, pos, omega, per_step_budget)
     times = []
     for k in range(args.warmup + args.steps):
@@ -505,6 +506,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=0.0,
+                    help="reference arm: CPU seconds of work per step (0: sized so the run takes ~1.5 min)")
     ap.add_argument("--precision", type=int, choices=[32, 64], default=32,
                     help="64: the plain FP64 path (field values, MIS terms, sums in FP64)")
     ap.add_argument("--deform", action="store_true",
