@@ -7,10 +7,19 @@
 #include "vortex_particle_mc.hpp"
 
 // Ax_cuda (src/cuda/cg_rbf_init.cu:33-50): y = A x over all particles of the
-// simulation (device pointers).  The SpMV runs on the library context and
-// completes before return, whatever `stream`.
+// simulation (device pointers).  The SpMV runs on the library context's
+// stream, ordered after the work already queued on `stream` (x may be produced
+// there), and completes before return, so later work on `stream` sees y.
 inline void Ax_cuda(const Simulation& sim, const float* x, float* y, cudaStream_t stream = 0) {
-    (void)stream;
+    cudaStream_t own = static_cast<cudaStream_t>(vpmc_context_stream(sim.ctx()));
+    if (stream != own) {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+            throw vpmc::error(VPMC_ERR_CUDA, "Ax_cuda: event");
+        const bool ok = cudaEventRecord(ev, stream) == cudaSuccess && cudaStreamWaitEvent(own, ev, 0) == cudaSuccess;
+        cudaEventDestroy(ev);
+        if (!ok) throw vpmc::error(VPMC_ERR_CUDA, "Ax_cuda: stream order");
+    }
     vpmc::check(vpmc_rbf_matvec(sim.ctx(), sim.particles_.N_cur, reinterpret_cast<const float*>(sim.particles_.d_p()),
                                 x, y, sim.P_.h_w, sim.P_.Lx, sim.P_.Ly, sim.P_.periodic ? 1 : 0, 1),
                 "Ax_cuda");

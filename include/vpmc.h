@@ -79,6 +79,16 @@ int vpmc_abi_version(void);
 /* Number of kernels this library has launched in this process (all contexts):
  * a counter for benchmarks that report GPU launch counts. */
 uint64_t vpmc_kernel_launch_count(void);
+/* Bounded device waits.  The field-evaluation kernel stages candidates with
+ * bulk copies and waits for them on an mbarrier; each wait polls at most
+ * `polls` times (default VPMC_WAIT_LIMIT_DEFAULT, far beyond any copy's
+ * latency), then the kernel lets the copy in flight land, stops, and the call
+ * returns VPMC_ERR_TIMEOUT with the context still usable.  0 makes every such
+ * wait give up at once: a way to exercise that error path without a fault.
+ * No reference counterpart (its only device check is an unused trap,
+ * src/utilities.cu:99-103). */
+#define VPMC_WAIT_LIMIT_DEFAULT (1u << 26)
+int vpmc_context_set_wait_limit(vpmc_context* ctx, uint32_t polls);
 
 /* --------------------------------------------------------------- hash (a1-a3)
  * Uniform-grid spatial hash of a particle subset, bit-exact with the
@@ -125,10 +135,15 @@ int vpmc_hash_build_host(vpmc_context* ctx, int rshx, int rshy, float Lx, float 
  * library that every GPU using the library holds until process exit.
  * Limits: N <= 262144 particles and rshx*rshy <= 1048576 cells, otherwise
  * VPMC_ERR_CAPACITY.  All calls share that scratch, so calls that overlap on
- * the GPU (two host threads, or two streams) race; consecutive calls are
- * safe.  The first call on a device looks up the scratch array's address:
- * make it before any stream capture.  Results are identical to
- * vpmc_hash_build (device pointers, same layouts). */
+ * the GPU (two host threads, or two streams) race; every call waits for its
+ * stream to finish before it returns (also on an error after work was
+ * queued), so consecutive calls are safe.  `stream` must belong to the
+ * current device (VPMC_ERR_INVALID otherwise).  The first call on a device
+ * looks up the scratch array's address and keeps it for the process: make
+ * it before any stream capture, and do not use this entry point after
+ * cudaDeviceReset or under a non-primary context (the kept address would be
+ * stale).  Results are identical to vpmc_hash_build (device pointers, same
+ * layouts). */
 int vpmc_hash_build_noalloc(void* stream, int rshx, int rshy, float Lx, float Ly, int N,
                             const int* sub, const float* pos, int* cell_num, int* cell_acc,
                             int* vp_cell, int* vp_sort);
@@ -408,6 +423,17 @@ int vpmc_sim_geometry(vpmc_sim* sim, long long* info);
  * reference counterpart (instrumentation: the in-support pair count of the
  * evaluation's roofline). */
 int vpmc_sim_read_samples(vpmc_sim* sim, long long first, long long count, long long* t0, float* xy);
+
+/* Field values of the same samples (HOST array of count doubles; the FP32
+ * path's values are widened): the smoothed |omega| field of the sample's sign
+ * subset at the sample point, as the MIS terms use it -- with the unbiased
+ * law the sum over the 3x3 periodic images {-1,0,1}^2 of the particles seen
+ * from the unwrapped point, with the reference law the periodic field at the
+ * wrapped point; 0 for a sample the law drops.  Same indexing and validity
+ * rules as vpmc_sim_read_samples.  No reference counterpart (parity
+ * instrumentation of queryVorticityAbs inside monte_carlo_bs_kernel_safe,
+ * src/cuda/monte_carlo_bs.cu:214-218). */
+int vpmc_sim_read_field(vpmc_sim* sim, long long first, long long count, long long* t0, double* f);
 
 /* ---------------------------------------------------------------- misc */
 /* Philox4x32-10 (Salmon et al., SC'11) block function, host evaluation:

@@ -25,7 +25,8 @@ __all__ = [
     "rcdf", "icdf", "spline_pdf", "spline_mass", "OracleState", "eval_vorticity_cpu",
     "query_vorticity_f64", "field_exact_f64", "mc_estimates", "mc_velocity", "mc_velocity_omp",
     "rbf_matvec_f64", "cg_rbf_f64", "direct_mollified_f64", "direct_plummer_f64", "direct_deformed_f64",
-    "mc_velocity5_omp", "mis_forward_f64",
+    "mc_velocity5_omp", "mis_forward_f64", "spline_w_f64", "field_tiled_f64", "rbf_matrix_f64",
+    "rbf_solve_f64",
     "ref_available", "ref_fill_cells", "ref_counting_sort", "ref_build_subsets",
     "ref_rcdf", "ref_icdf", "ref_eval_vorticity", "ref_mc_estimates", "gaussian_field",
 ]
@@ -368,6 +369,81 @@ def field_exact_f64(pos, w, pts, sign, use_signed, h_w, Lx=1.0, Ly=1.0, periodic
     lib().orc_field_exact_f64(_ptr(pos), _ptr(w), len(pos), _ptr(pts), len(pts), sign, int(use_signed),
                               h_w, Lx, Ly, int(periodic), _ptr(out))
     return out
+
+
+def spline_w_f64(r, h_w):
+    """cubicSplinePDF (include/utilities.hpp:7-17) in FP64, vectorised:
+    W = 40/(7 pi h^2) {6(q^3 - q^2) + 1 (q <= 1/2), 2(1 - q)^3 (q < 1), 0}."""
+    r = np.asarray(r, np.float64)
+    q = r / float(h_w)
+    s = 40.0 / (7.0 * np.pi * float(h_w) ** 2)
+    inner = 6.0 * (q ** 3 - q ** 2) + 1.0
+    outer = 2.0 * (1.0 - q) ** 3
+    return s * np.where(q <= 0.5, inner, np.where(q < 1.0, outer, 0.0))
+
+
+def field_tiled_f64(pos, w, pts, h_w, Lx=1.0, Ly=1.0, images=1):
+    """FP64 smoothed field sum_i sum_m w_i W(|p - x_i - m (Lx, Ly)|) at the
+    points p as given (not wrapped), over the periodic images m in
+    {-images..images}^2 of the particles (positions wrapped into the domain
+    first).  images = 1 at unwrapped MIS sample points is the field the
+    unbiased estimator weights with (the 3x3 images its branch-1 draw covers);
+    at wrapped points it is the periodic field of queryVorticityAbs
+    (include/vorticity_query.cuh:15-79, minimum image, W = 0 beyond h_w).
+    Pairs are found with a k-d tree (scipy), every in-support pair summed in
+    FP64."""
+    from scipy.spatial import cKDTree
+    L = np.array([Lx, Ly], np.float64)
+    p = np.mod(np.asarray(pos, np.float32).astype(np.float64), L)
+    w = np.asarray(w, np.float64)
+    pts = np.asarray(pts, np.float32).astype(np.float64)
+    out = np.zeros(len(pts))
+    if len(p) == 0 or len(pts) == 0:
+        return out
+    m = np.arange(-images, images + 1)
+    shifts = np.stack(np.meshgrid(m, m, indexing="ij"), -1).reshape(-1, 2) * L
+    src = (p[None, :, :] + shifts[:, None, :]).reshape(-1, 2)
+    ws = np.tile(w, len(shifts))
+    tree = cKDTree(src)
+    for k, nb in enumerate(tree.query_ball_point(pts, r=float(h_w))):
+        if nb:
+            nb = np.asarray(nb)
+            d = np.sqrt(((src[nb] - pts[k]) ** 2).sum(1))
+            out[k] = float(np.sum(ws[nb] * spline_w_f64(d, h_w)))
+    return out
+
+
+def rbf_matrix_f64(pos, h_w, Lx=1.0, Ly=1.0, periodic=True):
+    """The RBF system matrix of conjugate_gradient_rbf (src/cuda/cg_rbf_init.cu:
+    11-31: A_ij = W(|x_j - x_i|), nearest image, diagonal included) in FP64 as a
+    scipy CSR matrix."""
+    import scipy.sparse as sp
+    from scipy.spatial import cKDTree
+    L = np.array([Lx, Ly], np.float64)
+    p = np.asarray(pos, np.float32).astype(np.float64)
+    if periodic:
+        p = np.mod(p, L)
+        p = np.where(p >= L, p - L, p)
+    tree = cKDTree(p, boxsize=L if periodic else None)
+    pairs = tree.query_pairs(r=float(h_w), output_type="ndarray")
+    d = p[pairs[:, 0]] - p[pairs[:, 1]]
+    if periodic:
+        d -= L * np.round(d / L)
+    v = spline_w_f64(np.sqrt((d ** 2).sum(1)), h_w)
+    n = len(p)
+    rows = np.concatenate([pairs[:, 0], pairs[:, 1], np.arange(n)])
+    cols = np.concatenate([pairs[:, 1], pairs[:, 0], np.arange(n)])
+    vals = np.concatenate([v, v, np.full(n, spline_w_f64(0.0, h_w))])
+    return sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+
+
+def rbf_solve_f64(pos, b, h_w, Lx=1.0, Ly=1.0, periodic=True):
+    """Exact FP64 solution of the RBF system (sparse LU) and |b - A x| / |b|."""
+    import scipy.sparse.linalg as sla
+    A = rbf_matrix_f64(pos, h_w, Lx, Ly, periodic).tocsc()
+    b = np.asarray(b, np.float64)
+    x = sla.spsolve(A, b)
+    return x, float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
 
 
 def mc_estimates(state: OracleState, dst5, aux, N1, N2, seed):

@@ -57,6 +57,18 @@ int main(int argc, char** argv) {
         dvec<float> y{size_t(N)};
         Ax_cuda(sim, sim.particles_.d_omega(), raw_ptr(y));
         dump("Ax", y.to_host());
+        {
+            // x produced on a caller stream right before the call: Ax_cuda orders
+            // itself after that stream's work
+            cudaStream_t us = nullptr;
+            vpmc::check_cuda(cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking), "stream");
+            dvec<float> x2{size_t(N)}, y2{size_t(N)};
+            vpmc::check_cuda(cudaMemcpyAsync(raw_ptr(x2), sim.particles_.d_omega(), sizeof(float) * size_t(N),
+                                             cudaMemcpyDeviceToDevice, us), "copy x");
+            Ax_cuda(sim, raw_ptr(x2), raw_ptr(y2), us);
+            dump("Ax_stream", y2.to_host());
+            vpmc::check_cuda(cudaStreamDestroy(us), "stream");
+        }
 
         // reference-named free functions on the all-particle subset
         std::vector<int> iota(N);

@@ -66,6 +66,7 @@ def test_matvec_step_and_naive_step(run):
     st = O.OracleState(pos, omega, prm)
     want = O.rbf_matvec_f64(st, omega.astype(np.float64))
     assert np.abs(run("Ax", np.float32) - want).max() <= 2e-6 * np.abs(want).max()
+    assert np.array_equal(run("Ax_stream", np.float32), run("Ax", np.float32))   # Ax_cuda on a caller stream
     assert run("grid_err", np.float64)[0] < 1e-4 * np.abs(omega).max() * 100
     p1, v1 = run("pos1", np.float32).reshape(-1, 2), run("vel1", np.float32).reshape(-1, 2)
     assert np.isfinite(v1).all() and np.abs(v1).max() > 0

@@ -1,0 +1,131 @@
+"""The field evaluation at the benchmark's own tuning, value by value.
+
+The step benchmarked on 2048^2 runs the evaluation kernel with 15-17-column
+walks (k_walk 5-8 cells per h_w), chord-trimmed sub-row runs, per-warp box
+trimming and 4-8 queries per thread.  These tests run that kernel on a
+512^2 Taylor-Green lattice with hwr = 16 and N1 = N2 = 64 -- the benchmark's
+h_w in cells and its samples per target, so its queries per bin -- and read
+back the field value of every sample of a set of targets:
+
+  * unbiased law (FIELD9 mode): the 3x3-image field at the unwrapped sample
+    point, against the FP64 sum over the 3x3-tiled particles (oracle k-d tree);
+  * reference law (FIELD mode, the field queryVorticityAbs gives,
+    include/vorticity_query.cuh:15-79): the periodic field at the wrapped point;
+
+for every (k_walk, queries per thread) in {5, 6, 7, 8} x {4, 6, 8}, within 1e-5
+of the field's scale and, for every value above 1% of that scale, within 1e-5
+relative.  The velocities of all tunings agree target by target, and the
+unbiased estimator's 64-seed mean at k_walk = 7 lies within 3 standard errors
+of the FP64 mollified direct sum (src/cuda/monte_carlo_bs.cu:144-271 is the
+estimator these samples feed).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from conftest import to_dev
+
+pytestmark = pytest.mark.gpu
+
+NX, HWR, N1, N2 = 512, 16.0, 64, 64
+TUNINGS = [(k, q) for k in (5, 6, 7, 8) for q in (4, 6, 8)]
+N_TARGETS = 24          # 24 x 256 = 6144 sample values per law and tuning
+STEP = 3
+
+
+@pytest.fixture(scope="module")
+def tg512(cuda):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    pos = O.lattice(NX)
+    sp = P.SimParam(dt=5e-4, Nx=NX, hwr=HWR, N1=N1, N2=N2, law=P.LAW_UNBIASED, seed=11)
+    sim = P.Simulation(sp, [len(pos)])
+    sim.set_particles(to_dev(pos, cuda), torch.zeros(len(pos), device=cuda))
+    info = sim.init_strengths(None, tol=1e-8, max_iter=50)[0]
+    assert info["true_relres"] < 1e-6
+    _, om, _ = sim.particles()
+    yield sim, sp, pos, om.cpu().numpy()
+    sim.close()
+
+
+def _read(sim, targets, spt):
+    xy, f = [], []
+    for t in targets:
+        t0, a = sim.read_samples(int(t) * spt, spt)
+        assert t0 == 0
+        _, b = sim.read_field(int(t) * spt, spt)
+        xy.append(a)
+        f.append(b)
+    return np.stack(xy), np.stack(f)          # (targets, spt, 2), (targets, spt)
+
+
+def _oracle(pos, om, xy, h_w, law):
+    """FP64 field of the sample's own sign subset at each sample."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    spt = xy.shape[1]
+    want = np.zeros(xy.shape[:2])
+    for s, sel in enumerate((om > 0, om < 0)):
+        ys = xy[:, s * spt // 2:(s + 1) * spt // 2].reshape(-1, 2).astype(np.float64)
+        if law == P.LAW_UNBIASED:
+            k = np.floor(ys)
+            keep = np.all(np.abs(k) <= 2, 1)          # the law drops samples more than two periods out
+            pts = ys
+        else:
+            keep = np.ones(len(ys), bool)
+            pts = np.mod(ys, 1.0)
+        v = O.field_tiled_f64(pos[sel], np.abs(om[sel]), pts, h_w) * keep
+        want[:, s * spt // 2:(s + 1) * spt // 2] = v.reshape(len(xy), -1)
+    return want
+
+
+@pytest.mark.parametrize("law_name", ["unbiased", "reference"])
+def test_sample_field_values_every_tuning(tg512, law_name):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    sim, sp, pos, om = tg512
+    law = P.LAW_UNBIASED if law_name == "unbiased" else P.LAW_REFERENCE
+    sim.set_law(law)
+    spt = sim.geometry()["samples_per_target"]
+    assert spt == 2 * (N1 + N2)
+    targets = np.random.default_rng(3).choice(len(pos), N_TARGETS, replace=False)
+    xy0, want, vel0 = None, None, None
+    for k, q in TUNINGS:
+        sim.set_tuning(k, q)
+        assert sim.tuning() == (k, q)
+        vel = sim.velocity(step=STEP).cpu().numpy()
+        xy, got = _read(sim, targets, spt)
+        if xy0 is None:
+            xy0, vel0 = xy, vel
+            want = _oracle(pos, om, xy, sp.h_w, law)
+            assert (want > 0).mean() > 0.5           # most samples see their subset
+        # the samples do not depend on the tuning (same Philox streams)
+        assert np.array_equal(xy, xy0), (k, q)
+        scale = want.max()
+        err = np.abs(got - want)
+        assert err.max() <= 1e-5 * scale, (k, q, err.max() / scale)
+        big = want > 1e-2 * scale
+        rel = err[big] / want[big]
+        assert rel.max() <= 1e-5, (k, q, rel.max(), np.median(rel))
+        assert np.all(got[want == 0] == 0), (k, q)
+        # the velocities of all tunings agree target by target (FP32 rounding of
+        # the field sums; a wrong run of candidates would move a target by a few %)
+        rms = np.sqrt(np.mean(vel0 ** 2))
+        d = np.abs(vel - vel0).max(1) / rms
+        assert np.quantile(d, 0.999) <= 1e-4 and d.max() <= 1e-3, (k, q, np.quantile(d, 0.999), d.max())
+    sim.set_law(P.LAW_UNBIASED)
+
+
+def test_unbiased_mean_within_3se_at_benchmark_tuning(tg512, cuda):
+    from vortexparticlemc_cuda_gb300 import phash as P
+    sim, sp, pos, om = tg512
+    sim.set_law(P.LAW_UNBIASED)
+    sim.set_tuning(7, 4)
+    targets = np.random.default_rng(4).choice(len(pos), 512, replace=False)
+    tsel = torch.from_numpy(targets).to(cuda)
+    seeds = 64
+    v = np.stack([sim.velocity(step=100 + s)[tsel].cpu().numpy() for s in range(seeds)]).astype(np.float64)
+    truth = P.direct_velocity(to_dev(pos, cuda), to_dev(om, cuda), P.DIRECT_MOLLIFIED,
+                              pts=to_dev(pos[targets], cuda), param=sp.h_w).cpu().numpy()
+    z = (v.mean(0) - truth) / (v.std(0, ddof=1) / np.sqrt(seeds))
+    frac = np.mean(np.abs(z) <= 3.0)
+    assert frac >= 0.985, frac
+    assert 0.8 < np.mean(z ** 2) < 1.3, np.mean(z ** 2)

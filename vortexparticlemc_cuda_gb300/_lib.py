@@ -18,6 +18,7 @@ STATUS = {
     8: "VPMC_ERR_CAPACITY", 9: "VPMC_ERR_NOT_CONVERGED", 10: "VPMC_ERR_NONFINITE",
 }
 LAW_REFERENCE, LAW_UNBIASED = 0, 1
+WAIT_LIMIT_DEFAULT = 1 << 26   # VPMC_WAIT_LIMIT_DEFAULT
 DIRECT_MOLLIFIED, DIRECT_PLUMMER = 0, 1
 
 
@@ -50,6 +51,7 @@ SIGNATURES = {
     "vpmc_context_stream": (_vp, [_vp]),
     "vpmc_context_sync": (_i, [_vp]),
     "vpmc_context_scratch_bytes": (C.c_size_t, [_vp]),
+    "vpmc_context_set_wait_limit": (_i, [_vp, C.c_uint32]),
     "vpmc_fill_cells": (_i, [_vp, _i, _i, _f, _f, _i, _vp, _vp, _vp, _vp, _vp]),
     "vpmc_counting_sort": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
     "vpmc_hash_build": (_i, [_vp, _i, _i, _f, _f, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -97,6 +99,7 @@ SIGNATURES = {
     "vpmc_sim_last_stats": (_i, [_vp, _vp, _vp]),
     "vpmc_sim_geometry": (_i, [_vp, _vp]),
     "vpmc_sim_read_samples": (_i, [_vp, C.c_longlong, C.c_longlong, _vp, _vp]),
+    "vpmc_sim_read_field": (_i, [_vp, C.c_longlong, C.c_longlong, _vp, _vp]),
     "vpmc_philox4x32_10": (None, [_vp, _vp, _vp]),
 }
 

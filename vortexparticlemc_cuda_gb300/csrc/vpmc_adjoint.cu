@@ -355,6 +355,8 @@ int vpmc_sim_adjoint(vpmc_sim* s, const double* dL_dXT, double* dL_dX0, double* 
     vpmc_context* ctx = s->ctx;
     VPMC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
+    s->ys_t0 = -1;   // the adjoint redraws samples into the sample buffer
+    s->ys_nt = 0;
     AdjBufs A;
     VPMC_TRY(adj_bufs(s, &A));
     const int T = s->rec_steps, k = s->rec_k;

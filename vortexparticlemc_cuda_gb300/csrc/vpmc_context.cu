@@ -154,6 +154,12 @@ int vpmc_context_destroy(vpmc_context* c) {
 
 void* vpmc_context_stream(vpmc_context* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
 
+int vpmc_context_set_wait_limit(vpmc_context* c, uint32_t polls) {
+    if (!c) return VPMC_ERR_INVALID;
+    c->wait_limit = polls;
+    return VPMC_OK;
+}
+
 int vpmc_context_sync(vpmc_context* c) {
     if (!c) return VPMC_ERR_INVALID;
     VPMC_CUDA(cudaSetDevice(c->device));

@@ -15,7 +15,7 @@ constexpr int kEvalThreads = 32;
 constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
 constexpr int kCandCap = 200;                  // candidates staged per batch (6.25 KB: 24 one-warp CTAs per SM)
-constexpr uint32_t kWaitLimit = 1u << 26;      // mbarrier try_wait iterations before giving up
+constexpr uint32_t kWaitLimit = VPMC_WAIT_LIMIT_DEFAULT;   // drain wait of an aborted CTA (always the full cap)
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
     int lo = 0, hi = n_inst - 1;
@@ -603,6 +603,7 @@ struct EvalArgs {
     float* out_f32;
     double* out_f64;
     unsigned* flags;
+    uint32_t wait_limit;      // polls of a staging wait before the kernel gives up
 };
 
 // Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction
@@ -1015,7 +1016,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             }
             // each thread sees the copied bytes once its own wait completes; the
             // packed modes rewrite them first, so their barrier follows that pass
-            if (!mbar_wait_bounded(&s_bar, phase, kWaitLimit)) atomicOr(&s_abort, 1);
+            if (!mbar_wait_bounded(&s_bar, phase, a.wait_limit)) atomicOr(&s_abort, 1);
             phase ^= 1u;
             if constexpr (!kPacked) {
                 __syncthreads();
@@ -1581,7 +1582,7 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
     if (eval_deformed(L.mode) && !g.candf) return VPMC_ERR_INVALID;
     EvalArgs a{g.inst, g.start, L.rows > 0 ? L.rows : g.rows, g.cand, g.candf, qrec, it.items, it.n_items, it.counter,
-               L.out_f32, L.out_f64, ctx->d_flags};
+               L.out_f32, L.out_f64, ctx->d_flags, ctx->wait_limit};
     switch (L.mode) {
         case EVAL_FIELD:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);

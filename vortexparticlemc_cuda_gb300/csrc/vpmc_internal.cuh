@@ -84,6 +84,7 @@ struct vpmc_context {
     vpmc::DevBuf scratch[vpmc::kScratchSlots];
     unsigned* d_flags = nullptr;   // device error flags
     unsigned* h_flags = nullptr;   // pinned mirror
+    uint32_t wait_limit = VPMC_WAIT_LIMIT_DEFAULT;   // polls of a staging wait before it gives up
     // holders: the creator plus every simulation bound to the context; the
     // context is freed when the last one lets go (so destroying a context
     // before its simulations, as a garbage collector may, stays safe)

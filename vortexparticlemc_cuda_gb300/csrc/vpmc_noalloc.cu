@@ -12,10 +12,15 @@
 //
 // The array is shared by every call: a call overwrites what the previous one
 // left (nothing in it needs to start at zero), and two calls that overlap on
-// the GPU (different host threads or streams) race on it.  A call returns
-// after its stream has finished, so consecutive calls from one thread are
-// safe.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress); make that first call before any stream capture.
+// the GPU (different host threads or streams) race on it.  Every call waits
+// for its stream to finish before it returns -- also when it fails after
+// issuing work -- so consecutive calls from one thread are safe.  The first
+// call on a device looks up the array's device address (cudaGetSymbolAddress)
+// and keeps it for the life of the process; make that first call before any
+// stream capture.  The kept address belongs to the device's primary context:
+// after cudaDeviceReset, or under another context of the same device, it is
+// stale, so such callers must not use this entry point.  The stream must
+// belong to the current device (VPMC_ERR_INVALID otherwise).
 #include <mutex>
 
 #include "vpmc_internal.cuh"
@@ -67,6 +72,9 @@ extern "C" int vpmc_hash_build_noalloc(void* stream, int rshx, int rshy, float L
     if (long(N) > kMaxN || long(rshx) * long(rshy) > kMaxCells) return VPMC_ERR_CAPACITY;
     int dev = 0;
     VPMC_CUDA(cudaGetDevice(&dev));
+    int sdev = dev;
+    VPMC_CUDA(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev));
+    if (sdev != dev) return VPMC_ERR_INVALID;   // the scratch array used is the current device's
     void* base = nullptr;
     VPMC_TRY(scratch_address(dev, &base));
 
@@ -83,6 +91,13 @@ extern "C" int vpmc_hash_build_noalloc(void* stream, int rshx, int rshy, float L
     local.device = dev;
     local.stream = static_cast<cudaStream_t>(stream);
     cudaStream_t st = local.stream;
+    // from here on work is queued: whatever the outcome, the call returns only
+    // once the stream has drained, so no queued kernel still uses the shared
+    // scratch when the next call starts
+    struct DrainOnExit {
+        cudaStream_t st;
+        ~DrainOnExit() { (void)cudaStreamSynchronize(st); }
+    } drain{st};
 
     VPMC_CUDA(cudaMemsetAsync(cell_num, 0, sizeof(int) * size_t(ncell), st));
     const float inv_hx = rshx / Lx;   // FillCells_cpu's FP32 expressions

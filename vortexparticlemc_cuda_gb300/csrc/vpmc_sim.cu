@@ -1373,6 +1373,25 @@ int vpmc_sim_read_samples(vpmc_sim* s, long long first, long long count, long lo
     return vpmc_context_sync(s->ctx);
 }
 
+int vpmc_sim_read_field(vpmc_sim* s, long long first, long long count, long long* t0, double* f) {
+    if (!s || first < 0 || count < 0 || (count > 0 && !f)) return VPMC_ERR_INVALID;
+    if (s->ys_t0 < 0) return VPMC_ERR_INVALID;   // no pass has evaluated samples into the current buffer
+    if (t0) *t0 = s->ys_t0;
+    if (first + count > s->ys_nt * 2LL * samples_per(s)) return VPMC_ERR_INVALID;
+    if (count == 0) return VPMC_OK;
+    VPMC_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    if (s->precision == 64) {
+        VPMC_CUDA(cudaMemcpyAsync(f, s->fv64 + first, sizeof(double) * size_t(count), cudaMemcpyDeviceToHost, st));
+        return vpmc_context_sync(s->ctx);
+    }
+    std::vector<float> tmp(static_cast<size_t>(count));
+    VPMC_CUDA(cudaMemcpyAsync(tmp.data(), s->fv + first, sizeof(float) * size_t(count), cudaMemcpyDeviceToHost, st));
+    VPMC_TRY(vpmc_context_sync(s->ctx));
+    for (size_t i = 0; i < tmp.size(); ++i) f[i] = double(tmp[i]);
+    return VPMC_OK;
+}
+
 int vpmc_sim_geometry(vpmc_sim* s, long long* info) {
     if (!s || !info) return VPMC_ERR_INVALID;
     info[0] = s->N;
@@ -1413,6 +1432,8 @@ int vpmc_sim_reinit(vpmc_sim* s, double tol, int max_iter, double* info) {
         if (long(p.Nx) * Ny != s->counts[i]) return VPMC_ERR_INVALID;
     }
     if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
+    s->ys_t0 = -1;   // the field values of the last pass are overwritten below
+    s->ys_nt = 0;
     int worst = VPMC_OK;
     for (int i = 0; i < s->n_inst; ++i) {
         const vpmc_sim_params& p = s->prm[i];

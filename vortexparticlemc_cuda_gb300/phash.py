@@ -16,7 +16,8 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, SimParams, VpmcError, check, lib)
+from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, WAIT_LIMIT_DEFAULT, SimParams,
+                   VpmcError, check, lib)
 
 __all__ = [
     "fill_dummy", "Context", "context", "fill_cells", "counting_sort", "hash_build", "build_subsets",
@@ -52,6 +53,11 @@ class Context:
 
     def scratch_bytes(self) -> int:
         return int(lib().vpmc_context_scratch_bytes(self.h))
+
+    def set_wait_limit(self, polls: int = WAIT_LIMIT_DEFAULT):
+        """Polls of a staging wait in the field-evaluation kernel before the
+        call gives up with VPMC_ERR_TIMEOUT (0: at once)."""
+        check(lib().vpmc_context_set_wait_limit(self.h, int(polls)), "vpmc_context_set_wait_limit")
 
     def close(self):
         if getattr(self, "h", None):
@@ -405,6 +411,15 @@ class Simulation:
         check(lib().vpmc_sim_read_samples(self.h, int(first), int(count), C.byref(t0),
                                           xy.ctypes.data_as(C.c_void_p)), "vpmc_sim_read_samples")
         return t0.value, xy
+
+    def read_field(self, first: int, count: int):
+        """Field values the last MIS pass evaluated at the same samples as
+        read_samples: (the chunk's first target, a (count,) float64 array)."""
+        f = np.empty(int(count), dtype=np.float64)
+        t0 = C.c_longlong()
+        check(lib().vpmc_sim_read_field(self.h, int(first), int(count), C.byref(t0),
+                                        f.ctypes.data_as(C.c_void_p)), "vpmc_sim_read_field")
+        return t0.value, f
 
     # adjoint (common random numbers, checkpoints every k steps)
     def record(self, nsteps: int, k_ckpt: int = 20):
