@@ -206,6 +206,24 @@ int vpmc_cg_rbf_f64rhs(vpmc_context* ctx, int N, const float* pos, const double*
                        float* omega_out, float h_w, float Lx, float Ly, int periodic,
                        double tol, int max_iter, double* info);
 
+/* The same system solved by MINRES (Paige & Saunders 1975) instead of CG,
+ * from the same starting point w0 = b / W(0), with the FP64 SpMV and FP64
+ * vectors, dots and norms.  The RBF matrix is symmetric but indefinite (the
+ * cubic spline's 2-D symbol is negative at high wavenumbers) with eigenvalues
+ * near zero on both sides, where CG can stall or break down; MINRES
+ * minimises |b - A w| over the same Krylov space, so the residual falls
+ * monotonically.  Stops when the recursive |r|/|b| < tol.  info (HOST, may be
+ * NULL) = {iterations, recursive |r|/|b|, true |b - A w|/|b|}; returns
+ * VPMC_ERR_NOT_CONVERGED (with omega_out written) after max_iter.  No
+ * reference counterpart: an alternative to conjugate_gradient_rbf
+ * (src/cuda/cg_rbf_init.cu:53-116) for fields that are not lattice modes. */
+int vpmc_minres_rbf(vpmc_context* ctx, int N, const float* pos, const float* b,
+                    float* omega_out, float h_w, float Lx, float Ly, int periodic,
+                    double tol, int max_iter, double* info);
+int vpmc_minres_rbf_f64rhs(vpmc_context* ctx, int N, const float* pos, const double* b,
+                           float* omega_out, float h_w, float Lx, float Ly, int periodic,
+                           double tol, int max_iter, double* info);
+
 /* ------------------------------------------------------ direct sums (a11)
  * biot_savart_naive_kernel, src/cuda/naive_biot_savart.cu:15-40, in FP64.
  * VPMC_DIRECT_PLUMMER: targets are particle indices `tidx` (M of them),
@@ -264,6 +282,12 @@ int vpmc_sim_get_particles(vpmc_sim* sim, float* pos, float* omega, float* vel, 
  * info (HOST, may be NULL): 3 doubles per instance as vpmc_cg_rbf. */
 int vpmc_sim_init_strengths(vpmc_sim* sim, const float* omega_field, double tol,
                             int max_iter, double* info);
+
+/* Solver of the strength fits vpmc_sim_init_strengths and vpmc_sim_reinit
+ * make: VPMC_RBF_CG (default, the reference's conjugate_gradient_rbf) or
+ * VPMC_RBF_MINRES (vpmc_minres_rbf). */
+typedef enum vpmc_rbf_solver { VPMC_RBF_CG = 0, VPMC_RBF_MINRES = 1 } vpmc_rbf_solver;
+int vpmc_sim_set_rbf_solver(vpmc_sim* sim, int solver);
 
 /* Sign subsets + FP64 |omega| CDFs + sampling tables for every instance
  * (build_subsets_cuda).  Strengths are conserved, so this runs once after

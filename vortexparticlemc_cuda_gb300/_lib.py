@@ -19,6 +19,7 @@ STATUS = {
 }
 LAW_REFERENCE, LAW_UNBIASED = 0, 1
 WAIT_LIMIT_DEFAULT = 1 << 26   # VPMC_WAIT_LIMIT_DEFAULT
+RBF_CG, RBF_MINRES = 0, 1
 DIRECT_MOLLIFIED, DIRECT_PLUMMER = 0, 1
 
 
@@ -64,6 +65,9 @@ SIGNATURES = {
     "vpmc_rbf_matvec": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _i]),
     "vpmc_cg_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_cg_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
+    "vpmc_minres_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
+    "vpmc_minres_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
+    "vpmc_sim_set_rbf_solver": (_i, [_vp, _i]),
     "vpmc_direct_velocity_f64": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _d, _i, _vp]),
     "vpmc_direct_velocity_f32": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _f, _f, _f, _i, _vp]),
     "vpmc_sim_create": (_i, [_vp, _i, _vp, _vp, C.POINTER(_vp)]),

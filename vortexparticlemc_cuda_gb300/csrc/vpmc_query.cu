@@ -1,6 +1,8 @@
 // vpmc_query.cu -- vorticity queries at arbitrary points, the matrix-free RBF
-// SpMV and the CG strength solve, all on the evaluation grid of vpmc_grid.cu.
+// SpMV and the CG / MINRES strength solves, all on the evaluation grid of
+// vpmc_grid.cu.
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "vpmc_grid.cuh"
@@ -73,6 +75,27 @@ __global__ void k_axpby(const double* __restrict__ a, const double* __restrict__
                         double* __restrict__ out) {
     for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
         out[i] = sa * a[i] + sb * b[i];
+}
+
+// MINRES vector steps (FP64).
+// u = Av - alpha v - beta v_old  (the next Lanczos vector before normalisation)
+// (Av and u may be the same array: each element is read before it is written)
+__global__ void k_minres_u(const double* Av, const double* __restrict__ v, const double* __restrict__ v_old, long n,
+                           double alpha, double beta, double* u) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+        u[i] = Av[i] - alpha * v[i] - beta * v_old[i];
+}
+// w_new = (v - rho3 w_old - rho2 w) / rho1 (written over w_old), x += c w_new,
+// v_next = u / beta_n (written over v_old)
+__global__ void k_minres_step(const double* __restrict__ v, double* __restrict__ w_old, const double* __restrict__ w,
+                              double* __restrict__ x, const double* __restrict__ u, double* __restrict__ v_old, long n,
+                              double rho1, double rho2, double rho3, double c, double inv_beta_n) {
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const double wn = (v[i] - rho3 * w_old[i] - rho2 * w[i]) / rho1;
+        w_old[i] = wn;
+        x[i] += c * wn;
+        v_old[i] = u[i] * inv_beta_n;
+    }
 }
 
 // Working set for one single-instance grid plus self/point queries.
@@ -254,9 +277,106 @@ int cg_impl(vpmc_context* ctx, int N, const float* pos, const float* b, const do
     }
     return res < tol || bnorm == 0 ? VPMC_OK : VPMC_ERR_NOT_CONVERGED;
 }
+// MINRES (Paige & Saunders, SIAM J. Numer. Anal. 12, 1975) on the same
+// system as cg_impl: Lanczos vectors from the FP64 SpMV, Givens rotations on
+// the host, residual norm |eta| decreasing monotonically.  Unlike CG it needs
+// no definiteness, which the RBF matrix lacks (its spline symbol is negative
+// at high wavenumbers, with eigenvalues close to zero on both sides).
+int minres_impl(vpmc_context* ctx, int N, const float* pos, const float* b, const double* b64, float* omega_out,
+                float h_w, float Lx, float Ly, int periodic, double tol, int max_iter, double* info) {
+    if (!ctx || N < 0 || !(h_w > 0.f) || !(Lx > 0.f) || !(Ly > 0.f) || max_iter < 0) return VPMC_ERR_INVALID;
+    if (N == 0) {
+        if (info) { info[0] = 0; info[1] = 0; info[2] = 0; }
+        return VPMC_OK;
+    }
+    if (!pos || (!b && !b64) || !omega_out) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    Work w;
+    VPMC_TRY(setup(ctx, SLOT_CG, N, h_w, Lx, Ly, periodic, 0, 8, &w));
+    double *bs = w.vec[0], *x = w.vec[1], *v = w.vec[2], *v_old = w.vec[3], *wv = w.vec[4], *w_old = w.vec[5],
+           *u = w.vec[6], *tmp = w.vec[7];
+    VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), nullptr, SET_ONE_SIGNED));
+    VPMC_LAUNCH(k_self_queries, blocks_for(N), 256, 0, st, w.g.cand, w.g.perm, w.g.cstart, long(N),
+                uint32_t(w.g.nbins), 0, w.self);
+    VPMC_TRY(make_items(ctx, w.g, w.g.cstart, w.it, query_chunk(4)));
+    if (b64) VPMC_LAUNCH(k_gather_to_sorted_d, blocks_for(N), 256, 0, st, b64, w.g.perm, long(N), bs);
+    else VPMC_LAUNCH(k_gather_to_sorted, blocks_for(N), 256, 0, st, b, w.g.perm, long(N), bs);
+    const double diag = spline_w_d(0.0, double(h_w));   // the reference's starting point x0 = b / W(0)
+    VPMC_LAUNCH(k_axpby, blocks_for(N), 256, 0, st, bs, bs, long(N), 1.0 / diag, 0.0, x);
+    VPMC_TRY(spmv_sorted(ctx, w, x, u, true));
+    VPMC_LAUNCH(k_axpby, blocks_for(N), 256, 0, st, bs, u, long(N), 1.0, -1.0, tmp);   // r0 = b - A x0
+    double bb = 0.0, r0 = 0.0;
+    VPMC_TRY(host_dot(ctx, w, bs, nullptr, N, &bb));
+    VPMC_TRY(host_dot(ctx, w, tmp, nullptr, N, &r0));
+    const double bnorm = std::sqrt(bb);
+    double beta = std::sqrt(r0);
+    double eta = beta;                                   // |eta| = residual norm of the current iterate
+    int it = 0;
+    if (bnorm > 0 && beta > 0) {
+        VPMC_LAUNCH(k_axpby, blocks_for(N), 256, 0, st, tmp, tmp, long(N), 1.0 / beta, 0.0, v);
+        VPMC_CUDA(cudaMemsetAsync(v_old, 0, sizeof(double) * size_t(N), st));
+        VPMC_CUDA(cudaMemsetAsync(wv, 0, sizeof(double) * size_t(N), st));
+        VPMC_CUDA(cudaMemsetAsync(w_old, 0, sizeof(double) * size_t(N), st));
+        double g0 = 1.0, g1 = 1.0, s0 = 0.0, s1 = 0.0;   // the last two Givens rotations (cos, sin)
+        while (it < max_iter && std::fabs(eta) >= tol * bnorm) {
+            VPMC_TRY(spmv_sorted(ctx, w, v, u, true));
+            double alpha = 0.0;
+            VPMC_TRY(host_dot(ctx, w, v, u, N, &alpha));
+            VPMC_LAUNCH(k_minres_u, blocks_for(N), 256, 0, st, u, v, v_old, long(N), alpha, beta, u);
+            double bn2 = 0.0;
+            VPMC_TRY(host_dot(ctx, w, u, nullptr, N, &bn2));
+            const double beta_n = std::sqrt(bn2);
+            // QR of the tridiagonal Lanczos matrix, one column per iteration
+            const double delta = g1 * alpha - g0 * s1 * beta;
+            const double rho1 = std::hypot(delta, beta_n);
+            const double rho2 = s1 * alpha + g0 * g1 * beta;
+            const double rho3 = s0 * beta;
+            if (!(rho1 > 0.0) || !std::isfinite(rho1)) break;
+            g0 = g1;
+            s0 = s1;
+            g1 = delta / rho1;
+            s1 = beta_n / rho1;
+            VPMC_LAUNCH(k_minres_step, blocks_for(N), 256, 0, st, v, w_old, wv, x, u, v_old, long(N), rho1, rho2,
+                        rho3, g1 * eta, beta_n > 0.0 ? 1.0 / beta_n : 0.0);
+            std::swap(w_old, wv);   // w <- w_new, w_old <- w
+            std::swap(v_old, v);    // v <- u / beta_n, v_old <- v
+            eta = -s1 * eta;
+            beta = beta_n;
+            ++it;
+            if (beta_n == 0.0) break;   // the Krylov space is invariant: x is exact
+        }
+    }
+    // true residual with the FP64 SpMV
+    VPMC_TRY(spmv_sorted(ctx, w, x, u, true));
+    VPMC_LAUNCH(k_axpby, blocks_for(N), 256, 0, st, bs, u, long(N), 1.0, -1.0, tmp);
+    double ee = 0.0;
+    VPMC_TRY(host_dot(ctx, w, tmp, nullptr, N, &ee));
+    VPMC_LAUNCH(k_scatter_from_sorted, blocks_for(N), 256, 0, st, x, w.g.perm, long(N), omega_out);
+    VPMC_TRY(vpmc_context_sync(ctx));
+    const double res = bnorm > 0 ? std::fabs(eta) / bnorm : 0.0;
+    if (info) {
+        info[0] = it;
+        info[1] = res;
+        info[2] = bnorm > 0 ? std::sqrt(ee) / bnorm : 0.0;
+    }
+    return res < tol || bnorm == 0 ? VPMC_OK : VPMC_ERR_NOT_CONVERGED;
+}
 }  // namespace
 
 extern "C" {
+
+int vpmc_minres_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, float* omega_out, float h_w,
+                    float Lx, float Ly, int periodic, double tol, int max_iter, double* info) {
+    if (!b && N > 0) return VPMC_ERR_INVALID;
+    return minres_impl(ctx, N, pos, b, nullptr, omega_out, h_w, Lx, Ly, periodic, tol, max_iter, info);
+}
+
+int vpmc_minres_rbf_f64rhs(vpmc_context* ctx, int N, const float* pos, const double* b, float* omega_out, float h_w,
+                           float Lx, float Ly, int periodic, double tol, int max_iter, double* info) {
+    if (!b && N > 0) return VPMC_ERR_INVALID;
+    return minres_impl(ctx, N, pos, nullptr, b, omega_out, h_w, Lx, Ly, periodic, tol, max_iter, info);
+}
 
 int vpmc_cg_rbf(vpmc_context* ctx, int N, const float* pos, const float* b, float* omega_out, float h_w, float Lx,
                 float Ly, int periodic, double tol, int max_iter, double* info) {

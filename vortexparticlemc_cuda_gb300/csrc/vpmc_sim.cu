@@ -1172,13 +1172,15 @@ int vpmc_sim_init_strengths(vpmc_sim* s, const float* omega_field, double tol, i
         const long off = s->begin[i];
         const vpmc_sim_params& p = s->prm[i];
         double inf[3] = {0, 0, 0};
+        const bool mr = s->rbf_solver == VPMC_RBF_MINRES;
+        const float* pi = reinterpret_cast<const float*>(s->pos + off);
         const int rc = omega_field
-                           ? vpmc_cg_rbf(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off),
-                                         omega_field + off, s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol,
-                                         max_iter, inf)
-                           : vpmc_cg_rbf_f64rhs(ctx, s->counts[i], reinterpret_cast<const float*>(s->pos + off),
-                                                b + off, s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol,
-                                                max_iter, inf);
+                           ? (mr ? vpmc_minres_rbf : vpmc_cg_rbf)(ctx, s->counts[i], pi, omega_field + off,
+                                                                 s->omega + off, s->mc[i].hw, p.Lx, p.Ly, p.periodic,
+                                                                 tol, max_iter, inf)
+                           : (mr ? vpmc_minres_rbf_f64rhs : vpmc_cg_rbf_f64rhs)(ctx, s->counts[i], pi, b + off,
+                                                                               s->omega + off, s->mc[i].hw, p.Lx,
+                                                                               p.Ly, p.periodic, tol, max_iter, inf);
         if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) return rc;
         if (rc != VPMC_OK) worst = rc;
         if (info) { info[3 * i] = inf[0]; info[3 * i + 1] = inf[1]; info[3 * i + 2] = inf[2]; }
@@ -1262,6 +1264,12 @@ int vpmc_sim_set_precision(vpmc_sim* s, int bits) {
         VPMC_TRY(vpmc_sim_prepare(s));
     }
     return vpmc_context_sync(s->ctx);
+}
+
+int vpmc_sim_set_rbf_solver(vpmc_sim* s, int solver) {
+    if (!s || (solver != VPMC_RBF_CG && solver != VPMC_RBF_MINRES)) return VPMC_ERR_INVALID;
+    s->rbf_solver = solver;
+    return VPMC_OK;
 }
 
 int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
@@ -1453,8 +1461,9 @@ int vpmc_sim_reinit(vpmc_sim* s, double tol, int max_iter, double* info) {
         VPMC_LAUNCH(k_identity, blocks_for(n), 256, 0, st, s->F + b, n);
         // 3. strengths re-fitted by CG-RBF
         double inf[3] = {0, 0, 0};
-        const int rc = vpmc_cg_rbf(ctx, int(n), reinterpret_cast<const float*>(s->pos + b), s->fv, s->omega + b,
-                                   s->mc[i].hw, p.Lx, p.Ly, p.periodic, tol, max_iter, inf);
+        const int rc = (s->rbf_solver == VPMC_RBF_MINRES ? vpmc_minres_rbf : vpmc_cg_rbf)(
+            ctx, int(n), reinterpret_cast<const float*>(s->pos + b), s->fv, s->omega + b, s->mc[i].hw, p.Lx, p.Ly,
+            p.periodic, tol, max_iter, inf);
         if (rc != VPMC_OK && rc != VPMC_ERR_NOT_CONVERGED) return rc;
         if (rc != VPMC_OK) worst = rc;
         if (info) { info[3 * i] = inf[0]; info[3 * i + 1] = inf[1]; info[3 * i + 2] = inf[2]; }

@@ -127,6 +127,7 @@ struct vpmc_sim {
     double* cum64 = nullptr;           // per instance Omega_+-, x9 when periodic (FP64 path)
     std::vector<double> cum64_h;       // host copy (the working set is re-carved on re-planning)
     int precision = 32;
+    int rbf_solver = VPMC_RBF_CG;      // strength fits of init_strengths / reinit
     // deformation mode
     int deform = 0;
     float cover = 1.f;                 // plan cover: sigma_max(F) the walk reaches

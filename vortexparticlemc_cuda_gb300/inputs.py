@@ -47,3 +47,14 @@ def ensemble(n_inst: int = 64, sizes=(96, 128, 192, 256, 320, 384), K: int = 8, 
         pos.append(p)
         om.append(gaussian_vortices(p, c, a, r))
     return nxs, np.concatenate(pos), np.concatenate(om)
+
+
+def inverse_problem_field(pos: np.ndarray, seed: int = 7, n_vort: int = 4, amp_sd: float = 2.0,
+                          radius: float = 0.05) -> np.ndarray:
+    """True initial field of the inverse problem: Taylor-Green plus `n_vort`
+    Gaussian vortices (centres U[0,1)^2, amplitudes N(0, amp_sd^2), radius
+    `radius`, generator `seed`) (float32).  The guess is Taylor-Green alone."""
+    g = np.random.default_rng(seed)
+    c, a = g.random((n_vort, 2)), g.normal(0.0, amp_sd, n_vort)
+    return (taylor_green(pos).astype(np.float64)
+            + gaussian_vortices(pos, c, a, [radius] * n_vort).astype(np.float64)).astype(np.float32)

@@ -16,14 +16,14 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, WAIT_LIMIT_DEFAULT, SimParams,
-                   VpmcError, check, lib)
+from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED, RBF_CG, RBF_MINRES,
+                   WAIT_LIMIT_DEFAULT, SimParams, VpmcError, check, lib)
 
 __all__ = [
     "fill_dummy", "Context", "context", "fill_cells", "counting_sort", "hash_build", "build_subsets",
-    "kernel_icdf_table", "cubic_spline", "query_vorticity", "rbf_matvec", "cg_rbf", "direct_velocity",
+    "kernel_icdf_table", "cubic_spline", "query_vorticity", "rbf_matvec", "cg_rbf", "minres_rbf", "direct_velocity",
     "Simulation", "SimParam", "philox4x32_10", "launch_count", "LAW_REFERENCE", "LAW_UNBIASED",
-    "DIRECT_MOLLIFIED", "DIRECT_PLUMMER",
+    "DIRECT_MOLLIFIED", "DIRECT_PLUMMER", "RBF_CG", "RBF_MINRES",
 ]
 
 
@@ -221,6 +221,25 @@ def cg_rbf(pos, b, h_w, Lx=1.0, Ly=1.0, periodic=True, tol=5e-3, max_iter=1000, 
     return out, dict(iters=int(info[0]), relres=info[1], true_relres=info[2], converged=st == 0)
 
 
+def minres_rbf(pos, b, h_w, Lx=1.0, Ly=1.0, periodic=True, tol=1e-8, max_iter=5000, allow_unconverged=False):
+    """The RBF system of conjugate_gradient_rbf solved by MINRES (symmetric
+    indefinite matrix) -> (omega, info dict); b float32 or float64."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    if not isinstance(b, torch.Tensor) or not b.is_cuda:
+        raise TypeError("b must be a CUDA tensor")
+    b = b.contiguous()
+    out = torch.empty(b.shape[0], dtype=torch.float32, device=pos.device)
+    info = (C.c_double * 3)()
+    fn = lib().vpmc_minres_rbf_f64rhs if b.dtype == torch.float64 else lib().vpmc_minres_rbf
+    if b.dtype not in (torch.float32, torch.float64):
+        raise TypeError("b must be float32 or float64")
+    st = fn(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(b), _p(out), h_w, Lx, Ly, int(periodic), tol, max_iter,
+            C.cast(info, C.c_void_p))
+    if not (allow_unconverged and st == 9):
+        check(st, "vpmc_minres_rbf")
+    return out, dict(iters=int(info[0]), relres=info[1], true_relres=info[2], converged=st == 0)
+
+
 # ------------------------------------------------------------ direct sums (a11)
 def direct_velocity(pos, omega, kernel=DIRECT_MOLLIFIED, pts=None, tidx=None, param=0.04, Lx=1.0, Ly=1.0,
                     periodic=True):
@@ -348,6 +367,11 @@ class Simulation:
             check(st, "vpmc_sim_init_strengths")
         return [dict(iters=int(info[3 * i]), relres=info[3 * i + 1], true_relres=info[3 * i + 2])
                 for i in range(len(self.counts))]
+
+    def set_rbf_solver(self, solver: int):
+        """RBF_CG (the reference's conjugate_gradient_rbf) or RBF_MINRES for
+        init_strengths and reinit."""
+        check(lib().vpmc_sim_set_rbf_solver(self.h, int(solver)), "vpmc_sim_set_rbf_solver")
 
     def prepare(self):
         check(lib().vpmc_sim_prepare(self.h), "vpmc_sim_prepare")
