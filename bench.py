@@ -18,8 +18,11 @@ flush is needed between steps.
 restated bit-exactly in oracle/, OpenMP over targets on all host cores) on a
 bounded sample of targets of the same workload, one sample per step.
 
-Multi-GPU (torchrun): every rank runs its own replica of the workload (the
-path shards by independent instances; no collective), value = sum over ranks.
+Multi-GPU (torchrun): one job over all ranks (strong scaling).  A single
+simulation shards its targets over the ranks, each rank keeping every
+particle as a source, and all-gathers the updated positions after each step
+(NCCL); an ensemble splits its instances over the ranks with no collective.
+value = the job's particles x steps / the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -131,9 +134,10 @@ def max_over_ranks(x: float, device=None) -> float:
     return float(t.item())
 
 
-def replica_throughput(units_per_rank: int, world: int, steps: int, ms_max: float) -> float:
-    """Whole-job units/s of `world` independent replicas timed by the slowest."""
-    return units_per_rank * world * steps / (ms_max / 1e3)
+def job_throughput(units_per_job: int, steps: int, ms_max: float) -> float:
+    """Whole-job units/s: every unit of the job (all ranks together) per step,
+    timed by the slowest rank."""
+    return units_per_job * steps / (ms_max / 1e3)
 
 
 def reports(rank: int) -> bool:
@@ -141,18 +145,40 @@ def reports(rank: int) -> bool:
     return rank == 0
 
 
-def profile_traffic(workload: str):
-    """DRAM bytes per eval launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", f"k_eval_{workload}.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.lower().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one field-
+# evaluation launch, from ncu captures (a constant here: the bench cannot read
+# DRAM counters itself).  tg2048: the tg512s capture (same kernel, k_walk,
+# queries per thread and queries per bin on a 512^2 lattice, 1/16 of the
+# queries) scaled by the 16x queries -- the traffic grows in proportion:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
+#       -k regex:k_eval -s 1 -c 1 python bench.py --workload tg512s --k 7 --qpt 4 ...
+EVAL_DRAM_BYTES_PER_LAUNCH = {
+    "tg2048": {"bytes": 16 * 4.220e9, "source": "ncu capture of tg512s (4.220 GB per launch) x 16"},
+    "tg512s": {"bytes": 4.220e9, "source": "ncu capture of tg512s"},
+}
+
+
+def eval_traffic(workload: str):
+    t = EVAL_DRAM_BYTES_PER_LAUNCH.get(workload)
+    return None if t is None else t["bytes"]
+
+
+def cpu_model() -> str:
+    """CPU model name of this host (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 # ------------------------------------------------------------------ CPU side
@@ -218,7 +244,7 @@ def cpu_reference_sample(wl, pos, omega, budget_s, seed=17, nthreads=0, fixed_ta
     if fixed_targets is None:
         # a probe large enough to keep every host thread busy sizes the sample
         # to about budget_s seconds
-        n_probe = min(len(pos), 512)
+        n_probe = min(len(pos), 512 if nthreads <= 0 else 32 * nthreads)
         t_probe = pos[rng.choice(len(pos), n_probe, replace=False)]
         t0 = time.perf_counter()
         _, nt = O.mc_velocity_omp(st, t_probe, prm.N1, prm.N2, seed, nthreads)
@@ -232,6 +258,37 @@ def cpu_reference_sample(wl, pos, omega, budget_s, seed=17, nthreads=0, fixed_ta
     _ = targets + np.float32(prm.dt) * vel          # the Euler update of those targets
     dt = time.perf_counter() - t0
     return m / dt, nt, m, dt, st
+
+
+def cpu_hash_timings(wl, pos, omega, reps=3):
+    """The reference's per-step hash rebuild on the host (Simulation::
+    do_spatial_hashing: both sign subsets at rsh = Nx / hwr / 2 cells per axis)
+    with the oracle's bit-exact restatements: FillCells_cpu + CountingSort_cpu
+    (serial, src/cpu/hash.cpp:6-48) and FillCells_omp + CountingSort_omp (all
+    host threads, src/omp/hash_omp.cpp:12-70, whose sort output is incorrect).
+    Returns ms per rebuild (best of `reps`) and the threads used."""
+    import oracle as O
+    prm = O.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"])
+    s = O.build_subsets(omega)
+    px = np.ascontiguousarray(pos[:, 0])
+    py = np.ascontiguousarray(pos[:, 1])
+    out = {"rsh": prm.rshx, "particles_per_rebuild": int(s["cnt_pos"] + s["cnt_neg"])}
+    for kind in ("cpu", "omp"):
+        best, nt = 1e30, 1
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            for sub in (s["sub_pos"], s["sub_neg"]):
+                if kind == "cpu":
+                    cn, ca, vc = O.fill_cells(prm.rshx, prm.rshy, prm.Lx, prm.Ly, sub, px, py)
+                    O.counting_sort(cn, ca, vc)
+                else:
+                    cn, ca, vc, nt = O.fill_cells_omp(prm.rshx, prm.rshy, prm.Lx, prm.Ly, sub, px, py)
+                    O.counting_sort_omp(cn, ca, vc)
+            best = min(best, time.perf_counter() - t0)
+        out[kind] = {"ms_per_rebuild": 1e3 * best, "threads": nt if kind == "omp" else 1,
+                     "particles_per_s": out["particles_per_rebuild"] / best}
+    out["omp"]["note"] = "CountingSort_omp's output is incorrect (previous-cell base, hash_omp.cpp:65)"
+    return out
 
 
 def strengths_cpu(wl, pos, b):
@@ -313,18 +370,40 @@ def run_gpu(args, wl):
 
     law = P.LAW_UNBIASED if args.law == "unbiased" else P.LAW_REFERENCE
     ens = wl.get("ensemble", 0)
+    sharded = None
     if ens:
         nxs, pos, field = In.ensemble(ens)
         counts = [nx * nx for nx in nxs]
-        sps = [P.SimParam(dt=wl["dt"], Nx=nx, hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law,
-                          seed=1000 * rank + i) for i, nx in enumerate(nxs)]
+        n_job = len(pos)
+        if world > 1:
+            # instances split over ranks by particle count, no collective
+            from vortexparticlemc_cuda_gb300.shard import partition_instances
+            mine = partition_instances(counts, world)[rank]
+            starts = np.concatenate([[0], np.cumsum(counts)])
+            pos = np.concatenate([pos[starts[i]:starts[i + 1]] for i in mine])
+            field = np.concatenate([field[starts[i]:starts[i + 1]] for i in mine])
+            nxs = [nxs[i] for i in mine]
+            counts = [counts[i] for i in mine]
+            inst_ids = mine
+        else:
+            inst_ids = list(range(len(nxs)))
+        sps = [P.SimParam(dt=wl["dt"], Nx=nx, hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=i)
+               for i, nx in zip(inst_ids, nxs)]
     else:
         nxs, pos, field = [wl["Nx"]], In.lattice(wl["Nx"]), None
         counts = [len(pos)]
-        sps = [P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=rank)]
+        n_job = len(pos)
+        sps = [P.SimParam(dt=wl["dt"], Nx=wl["Nx"], hwr=wl["hwr"], N1=wl["N1"], N2=wl["N2"], law=law, seed=0)]
     N = len(pos)
     sp = sps[0]
-    sim = P.Simulation(sps, counts)
+    if world > 1 and not ens:
+        # one simulation, targets sharded over the ranks, positions all-gathered after each step
+        from vortexparticlemc_cuda_gb300.shard import ShardedSimulation
+        sharded = ShardedSimulation(sps, counts, rank, world, device=local)
+        sim = sharded.sim
+    else:
+        sim = P.Simulation(sps, counts)
+    step1 = (lambda: sharded.step(1)) if sharded else (lambda: sim.step(1, use_graph=True))  # noqa: E731
     tune = None
     pos_d = torch.from_numpy(pos).to(dev)
     sim.set_particles(pos_d, torch.zeros(N, device=dev))
@@ -379,7 +458,8 @@ def run_gpu(args, wl):
     log(f"accuracy: {err}")
     geo = sim.geometry()
     sim.set_step(0)
-    sim.step(args.warmup, use_graph=True)
+    for _ in range(args.warmup):
+        step1()
     stream = torch.cuda.current_stream(dev)
     if world > 1:
         dist.barrier()
@@ -389,7 +469,7 @@ def run_gpu(args, wl):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            sim.step(1, use_graph=True)
+            step1()
             eval_ms.append(sim.last_stats()["eval_ms"])
         e1.record(stream)
         torch.cuda.synchronize(dev)
@@ -404,7 +484,7 @@ def run_gpu(args, wl):
     n_hit = in_support_pairs(sim, sps, counts)
     log(f"in-support pairs per sample query: {n_hit:.1f}")
     ms = max_over_ranks(ms, dev)
-    value = replica_throughput(N, world, args.steps, ms)
+    value = job_throughput(n_job, args.steps, ms)
 
     # end to end through the host-buffer C-ABI call
     pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
@@ -412,18 +492,37 @@ def run_gpu(args, wl):
     hp_out = pin(np.zeros_like(pos))
     hv_out = pin(np.zeros_like(pos))
     a_in, a_out, a_vel = hp_in.numpy(), hp_out.numpy(), hv_out.numpy()
-    sim.step_host(a_in, a_out, a_vel)        # warm
+    d2h = int(2 * pos.nbytes)
+
+    def e2e_step(a_in, a_out, a_vel):
+        if sharded is None:
+            sim.step_host(a_in, a_out, a_vel)
+            return
+        # H2D + this rank's shard step, the position all-gather, D2H of all
+        # positions and of the shard's velocities
+        sim.step_host(a_in, None, None)
+        sharded.send_buffer()
+        sharded.ex.allgather(sharded.ex.recv, sharded.ex.send)
+        sharded.receive()
+        torch.from_numpy(a_out).copy_(sharded.full)
+        b, e = sharded.ex.begin, sharded.ex.end
+        torch.from_numpy(a_vel[b:e]).copy_(sim.particles()[2][b:e])
+
+    if sharded is not None:
+        d2h = int(pos.nbytes + 8 * (sharded.ex.end - sharded.ex.begin))
+    e2e_step(a_in, a_out, a_vel)        # warm
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        sim.step_host(a_in, a_out, a_vel)
+        e2e_step(a_in, a_out, a_vel)
         a_in, a_out = a_out, a_in
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
     e2e_ms = max_over_ranks(1e3 * e2e_s, dev)
-    e2e = {"value": replica_throughput(N, world, args.e2e_steps, e2e_ms), "unit": "particle-steps/s",
-           "h2d_bytes_per_step": int(pos.nbytes), "d2h_bytes_per_step": int(2 * pos.nbytes),
-           "steps": args.e2e_steps, "call": "vpmc_sim_step_host (pinned host buffers)"}
+    e2e = {"value": job_throughput(n_job, args.e2e_steps, e2e_ms), "unit": "particle-steps/s",
+           "h2d_bytes_per_step": int(pos.nbytes), "d2h_bytes_per_step": d2h,
+           "steps": args.e2e_steps,
+           "call": "vpmc_sim_step_host (pinned host buffers)" + (" + position all-gather" if sharded else "")}
 
     # roofline of the dominant kernel (field evaluation, FP32-pipe bound)
     peaks, peak_kind = measured_peaks()
@@ -441,7 +540,8 @@ def run_gpu(args, wl):
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
             "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
                            f"({peak_kind}); the kernel is FP32-pipe bound: no tensor-core or HBM bound applies",
-            "traffic": None if args.deform else profile_traffic(args.workload),
+            "traffic": None if args.deform else eval_traffic(args.workload),
+            "traffic_source": None if args.deform else EVAL_DRAM_BYTES_PER_LAUNCH.get(args.workload, {}).get("source"),
             "algorithmic": f"{samples_launch:.0f} sample queries/launch x {n_hit:.1f} in-support pairs x 16 flop",
             "in_support_pairs": ("same-sign particles within h_w of the wrapped sample point (" +
                                  ("isotropic radius, " if args.deform else "") +
@@ -454,15 +554,21 @@ def run_gpu(args, wl):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         n0 = counts[0]   # an ensemble's baseline runs on instance 0
-        rate, nt, m, dt, _ = cpu_reference_sample(dict(wl, Nx=nxs[0]), pos[:n0], omega_d[:n0].cpu().numpy(),
-                                                  args.cpu_budget)
+        wl0 = dict(wl, Nx=nxs[0])
+        om0 = omega_d[:n0].cpu().numpy()
+        rate, nt, m, dt, st0 = cpu_reference_sample(wl0, pos[:n0], om0, args.cpu_budget)
+        rate1, _, m1, dt1, _ = cpu_reference_sample(wl0, pos[:n0], om0, args.cpu_budget / 2, nthreads=1, st=st0)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": nt, "kind": "port",
                "sample": f"{m} random targets ({dt:.1f} s), both signs, aux=0, Euler update, reference CPU "
-                         f"estimator (monte_carlo_bs_cpu restated in oracle/, bit-exact), OpenMP over targets"}
+                         f"estimator (monte_carlo_bs_cpu restated in oracle/, bit-exact), OpenMP over targets",
+               "value_1_core": rate1, "sample_1_core": f"{m1} random targets ({dt1:.1f} s) on one thread",
+               "cpu_model": cpu_model(), "host_threads": os.cpu_count(),
+               "hash_rebuild": cpu_hash_timings(wl0, pos[:n0], om0)}
+        log(f"CPU baseline: {cpu}")
 
     out = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f64" if args.precision == 64 else "f32",
         "data": ("synthetic (64 Gaussian-vortex lattices, strengths from CG-RBF)" if ens
                  else "synthetic (Taylor-Green lattice, strengths from CG-RBF)"),
@@ -473,7 +579,9 @@ def run_gpu(args, wl):
                    "queries_per_thread": sim.tuning()[1],
                    "l2": f"inputs larger than L2 ({N * Q * 16 / 1e9:.1f} GB of sample records + "
                          f"{N * 32 / 1e6:.0f} MB candidates per step)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                   "parallelism": ("single GPU" if world == 1 else
+                                   (f"instances split over {world} ranks (no collective)" if ens else
+                                    f"targets sharded over {world} ranks, positions all-gathered per step"))},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -181,6 +181,15 @@ int vpmc_query_vorticity(vpmc_context* ctx, int N, const float* pos, const float
                          int use_signed, int exclude_center, float h_w, float Lx,
                          float Ly, int periodic, float* out);
 
+/* The same query with every pair and the sum in FP64 (the plain FP64 GPU path
+ * of the query: the FP32 strengths, split exactly into two floats, times the
+ * spline evaluated in FP64); isotropic kernels only, no exclude_center.
+ * out: M doubles (device).  No reference counterpart (an FP64 comparison
+ * path for queryVorticityAbs, include/vorticity_query.cuh:15-79). */
+int vpmc_query_vorticity_f64(vpmc_context* ctx, int N, const float* pos, const float* omega,
+                             int M, const float* pts, int sign, int use_signed, float h_w,
+                             float Lx, float Ly, int periodic, double* out);
+
 /* ---------------------------------------------------------- RBF / CG (a10)
  * Ax_cuda, src/cuda/cg_rbf_init.cu:33-50 (matvec_kernel :11-31):
  *   y_i = sum_j x_j W(|x_j - x_i|; h_w) over all particles (nearest image).
@@ -394,6 +403,19 @@ int vpmc_sim_record(vpmc_sim* sim, int nsteps, int k_ckpt);
 enum { VPMC_ADJ_SCORE = 1 };
 int vpmc_sim_adjoint(vpmc_sim* sim, const double* dL_dXT, double* dL_dX0, double* dL_domega, int flags);
 int vpmc_sim_freeze_sampling(vpmc_sim* sim, int on);
+
+/* Shard of the targets: MIS passes (steps, velocity passes) estimate and
+ * advect only the particles [begin, end) of the instance-concatenated order;
+ * every particle stays a source (the hash and the field cover all N).  A
+ * target's samples depend only on its instance, its instance-local index and
+ * the step (the Philox counter), so a shard's velocities and positions are
+ * bit-identical to the whole run's as long as all positions agree: a sharded
+ * run on several GPUs all-gathers the updated positions after each step.
+ * Particles outside the range keep their positions and velocities.  Not with
+ * deformation mode or the adjoint (VPMC_ERR_UNSUPPORTED).  Default: [0, N).
+ * No reference counterpart (the reference runs on one GPU). */
+int vpmc_sim_set_target_range(vpmc_sim* sim, long long begin, long long end);
+int vpmc_sim_get_target_range(vpmc_sim* sim, long long* begin, long long* end);
 
 /* Change the estimator law / seed / step counter of an existing simulation. */
 int vpmc_sim_set_law(vpmc_sim* sim, int law);

@@ -1,15 +1,15 @@
 #!/usr/bin/env bash
 # Build oracle/_ref/libvpmc_ref.so from the reference's own CPU sources, read
-# in place from the reference tree (default /root/reference, override with
-# VPMC_REFERENCE_DIR), plus oracle/ref_shim.cpp.  Test infrastructure only:
-# the output is git-ignored and used to pin the oracle and make golden
-# vectors.  Exits 0 without building when the reference tree is absent.
+# in place from the reference tree named by VPMC_REFERENCE_DIR, plus
+# oracle/ref_shim.cpp.  Test infrastructure only: the output is git-ignored
+# and used to pin the oracle and make golden vectors.  Exits 0 without
+# building when VPMC_REFERENCE_DIR is unset or holds no reference tree.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${VPMC_REFERENCE_DIR:-/root/reference}"
+ref="${VPMC_REFERENCE_DIR:-}"
 out="$here/_ref"
-if [ ! -d "$ref/src/cpu" ]; then
-    echo "build_ref: reference tree not found at $ref; skipping" >&2
+if [ -z "$ref" ] || [ ! -d "$ref/src/cpu" ]; then
+    echo "build_ref: no reference tree (set VPMC_REFERENCE_DIR); skipping" >&2
     exit 0
 fi
 mkdir -p "$out/stub/thrust"

@@ -21,7 +21,8 @@ REF_SO = os.path.join(HERE, "_ref", "libvpmc_ref.so")
 
 __all__ = [
     "build", "build_ref", "lib", "ref_lib", "SimParam", "lattice", "taylor_green",
-    "fill_cells", "counting_sort", "hash_build", "build_subsets", "build_subsets_f64",
+    "fill_cells", "counting_sort", "fill_cells_omp", "counting_sort_omp", "hash_build", "build_subsets",
+    "build_subsets_f64",
     "rcdf", "icdf", "spline_pdf", "spline_mass", "OracleState", "eval_vorticity_cpu",
     "query_vorticity_f64", "field_exact_f64", "mc_estimates", "mc_velocity", "mc_velocity_omp",
     "rbf_matvec_f64", "cg_rbf_f64", "direct_mollified_f64", "direct_plummer_f64", "direct_deformed_f64",
@@ -96,6 +97,8 @@ def lib():
         sig = {
             "orc_fill_cells": (None, [ip, ip, fl, fl, ip, vp, vp, vp, vp, vp, vp]),
             "orc_counting_sort": (None, [ip, vp, vp, vp, vp]),
+            "orc_fill_cells_omp": (ip, [ip, ip, fl, fl, ip, vp, vp, vp, vp, vp, vp, ip]),
+            "orc_counting_sort_omp": (ip, [ip, vp, vp, vp, vp, ip]),
             "orc_build_subsets": (None, [ip, vp, vp, vp, vp, vp, vp, vp]),
             "orc_build_subsets_f64": (None, [ip, vp, vp, vp, vp, vp, vp, vp]),
             "orc_build_cubic_rcdf": (None, [fl, ip, vp]),
@@ -240,6 +243,33 @@ def counting_sort(cell_num, cell_acc, vp_cell):
     vs = np.zeros(max(N, 1), np.int32)
     lib().orc_counting_sort(N, _ptr(cn), _ptr(ca), _ptr(vc), _ptr(vs))
     return cn, vs[:N]
+
+
+def fill_cells_omp(rshx, rshy, Lx, Ly, sub, px, py, nthreads=0):
+    """FillCells_omp restated (src/omp/hash_omp.cpp:12-54); -> (cell_num,
+    cell_acc, vp_cell, threads used)."""
+    sub = np.ascontiguousarray(sub, np.int32)
+    px = np.ascontiguousarray(px, np.float32)
+    py = np.ascontiguousarray(py, np.float32)
+    N = len(sub)
+    cn = np.zeros(rshx * rshy, np.int32)
+    ca = np.zeros(rshx * rshy, np.int32)
+    vc = np.zeros(max(N, 1), np.int32)
+    nt = lib().orc_fill_cells_omp(rshx, rshy, Lx, Ly, N, _ptr(sub), _ptr(px), _ptr(py), _ptr(cn), _ptr(ca),
+                                  _ptr(vc), int(nthreads))
+    return cn, ca, vc[:N], nt
+
+
+def counting_sort_omp(cell_num, cell_acc, vp_cell, nthreads=0):
+    """CountingSort_omp restated (src/omp/hash_omp.cpp:56-70, including its
+    previous-cell base, so vp_sort is wrong as the reference's is); -> (cell_num
+    after, vp_sort, threads used).  Unwritten slots of vp_sort stay 0."""
+    cn = np.array(cell_num, np.int32)
+    ca = np.ascontiguousarray(cell_acc, np.int32)
+    vc = np.ascontiguousarray(vp_cell, np.int32)
+    vs = np.zeros(max(len(vc), 1), np.int32)
+    nt = lib().orc_counting_sort_omp(len(vc), _ptr(cn), _ptr(ca), _ptr(vc), _ptr(vs), int(nthreads))
+    return cn, vs[:len(vc)], nt
 
 
 def hash_build(rshx, rshy, Lx, Ly, sub, pos):

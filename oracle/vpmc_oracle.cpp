@@ -395,6 +395,60 @@ void orc_counting_sort(int N, int* cell_num, const int* cell_acc,
     }
 }
 
+int orc_fill_cells_omp(int rshx, int rshy, float Lx, float Ly, int N, const int* sub, const float* px,
+                       const float* py, int* cell_num, int* cell_acc, int* vp_cell, int nthreads) {
+    const int ncell = rshx * rshy;
+    std::fill(cell_num, cell_num + ncell, 0);
+    const float inv_hx = rshx / Lx;
+    const float inv_hy = rshy / Ly;
+    int used = 1;
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+    {
+#pragma omp single
+        used = omp_get_num_threads();
+        std::vector<int> local(size_t(ncell), 0);
+#pragma omp for schedule(static)
+        for (int i = 0; i < N; ++i) {
+            const int j = sub[i];
+            const int ix = std::clamp(floor_to_int(px[j] * inv_hx), 0, rshx - 1);
+            const int iy = std::clamp(floor_to_int(py[j] * inv_hy), 0, rshy - 1);
+            const int c = ix * rshy + iy;
+            vp_cell[i] = c;
+            ++local[size_t(c)];
+        }
+#pragma omp critical
+        for (int c = 0; c < ncell; ++c) cell_num[c] += local[size_t(c)];
+    }
+    int acc = 0;
+    for (int c = 0; c < ncell; ++c) {
+        cell_acc[c] = acc;
+        acc += cell_num[c];
+    }
+    return used;
+}
+
+int orc_counting_sort_omp(int N, int* cell_num, const int* cell_acc, const int* vp_cell, int* vp_sort,
+                          int nthreads) {
+    int used = 1;
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+    {
+#pragma omp single
+        used = omp_get_num_threads();
+#pragma omp for schedule(static)
+        for (int i = N - 1; i >= 0; --i) {
+            const int c = vp_cell[i];
+            const int base = c == 0 ? 0 : cell_acc[c - 1];
+            int old;
+#pragma omp atomic capture
+            old = cell_num[c]--;
+            vp_sort[old - 1 + base] = i;
+        }
+    }
+    return used;
+}
+
 void orc_build_subsets(int N, const float* omega, int* sub_pos, int* sub_neg,
                        float* cdf_pos, float* cdf_neg, int* cnt, float* cum) {
     int np = 0, nn = 0;

@@ -63,6 +63,21 @@ void orc_fill_cells(int rshx, int rshy, float Lx, float Ly, int N,
 void orc_counting_sort(int N, int* cell_num, const int* cell_acc,
                        const int* vp_cell, int* vp_sort);
 
+/* ---- the OpenMP pair: src/omp/hash_omp.cpp:12-54 and :56-70 ----
+ * FillCells_omp: per-thread cell histograms merged under a critical section,
+ * then the exclusive scan (results equal FillCells_cpu's).  CountingSort_omp:
+ * reverse loop over particles split statically over threads, each slot taken
+ * by an atomic fetch-sub on cell_num, based at the PREVIOUS cell's offset
+ * cell_acc[c-1] (hash_omp.cpp:65) -- so its vp_sort is wrong (runs of
+ * neighbouring cells overwrite each other), as the reference's is; every
+ * store stays inside [0, N).  Kept for the timed CPU baseline only.
+ * nthreads <= 0 uses OpenMP's default; returns the threads used. */
+int orc_fill_cells_omp(int rshx, int rshy, float Lx, float Ly, int N,
+                       const int* sub, const float* px, const float* py,
+                       int* cell_num, int* cell_acc, int* vp_cell, int nthreads);
+int orc_counting_sort_omp(int N, int* cell_num, const int* cell_acc,
+                          const int* vp_cell, int* vp_sort, int nthreads);
+
 /* ---- sign subsets + |omega| CDF: src/cpu/build_particle_sets.cpp:6-42 ---- */
 void orc_build_subsets(int N, const float* omega,
                        int* sub_pos, int* sub_neg,

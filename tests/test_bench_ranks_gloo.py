@@ -1,7 +1,8 @@
-"""The multi-GPU path of bench.py is independent replicas (no data-path
-collective): each rank times its own simulation, the job time is the slowest
-rank's, the value is the work of all ranks over that time, and only rank 0
-reports.  Checked here with two gloo ranks on the CPU."""
+"""The multi-GPU timing of bench.py: one job over all ranks (targets sharded,
+or an ensemble's instances split), the job time is the slowest rank's, the
+value is the whole job's work over that time, and only rank 0 reports.
+Checked here with two gloo ranks on the CPU (the sharding itself:
+tests/test_shard_gloo.py)."""
 import os
 import socket
 
@@ -22,15 +23,15 @@ def _rank(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        ms = 100.0 + 50.0 * rank                      # rank 1 is the slow replica
+        ms = 100.0 + 50.0 * rank                      # rank 1 is the slow rank
         ms_max = bench.max_over_ranks(ms)
         dist.barrier()
-        q.put((rank, ms_max, bench.replica_throughput(1000, world, 4, ms_max), bench.reports(rank)))
+        q.put((rank, ms_max, bench.job_throughput(2000, 4, ms_max), bench.reports(rank)))
     finally:
         dist.destroy_process_group()
 
 
-def test_two_gloo_replicas_take_the_slowest_rank():
+def test_two_gloo_ranks_take_the_slowest_rank():
     world, port = 2, _free_port()
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -50,4 +51,4 @@ def test_two_gloo_replicas_take_the_slowest_rank():
 def test_single_process_needs_no_group():
     import bench
     assert bench.max_over_ranks(3.5) == 3.5
-    assert bench.replica_throughput(10, 1, 2, 1000.0) == 20.0
+    assert bench.job_throughput(10, 2, 1000.0) == 20.0

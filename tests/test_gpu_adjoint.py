@@ -5,7 +5,8 @@ checkpoints) against FP64 references.
     on 32 random strengths, and on initial positions) of the same estimator
     restated in FP64 on the CPU with the sampling law frozen (the discrete
     CDF-index choices of the pathwise derivative), both laws, across
-    checkpoint segments;
+    checkpoint segments, for the FP64 path and for the FP32-compensated
+    product path (whose adjoint runs along its own FP32 trajectory);
   * with the score-function term, the mean over 64 seeds of the adjoint
     gradient lies within 3 standard errors of the gradient of the FP64
     direct-sum solver (the estimator's mean) at Nx = 48;
@@ -39,10 +40,13 @@ def _sim(cuda, law, Nx=24, hwr=4, N1=8, N2=8, dt=2e-3, seed=3, precision=64, per
     return sim, pos, om, prm
 
 
-@pytest.mark.parametrize("law,periodic", [(0, True), (1, True), (1, False)])
-def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law, periodic):
+@pytest.mark.parametrize("law,periodic,precision", [(0, True, 64), (1, True, 64), (1, False, 64),
+                                                    (1, True, 32), (0, True, 32)])
+def test_pathwise_adjoint_matches_fp64_finite_differences(cuda, law, periodic, precision):
+    """precision 32: the adjoint of the FP32-compensated step (the product
+    path) against FP64 finite differences of the FP64 restatement."""
     T, K, seed = 6, 4, 3
-    sim, pos, om, prm = _sim(cuda, law, seed=seed, periodic=periodic)
+    sim, pos, om, prm = _sim(cuda, law, seed=seed, periodic=periodic, precision=precision)
     sim.freeze_sampling(True)
     rng = np.random.default_rng(7)
     fwd = lambda p, w, **kw: O.mis_forward_f64(p, w, prm, law, seed, T, periodic=periodic, **kw)   # noqa: E731

@@ -38,6 +38,27 @@ def test_query_matches_fp64_field(cuda, Nx, hwr):
     assert _rel(got, want) < 1e-5
 
 
+@pytest.mark.parametrize("Nx,hwr", [(256, 16), (512, 16)])
+def test_query_hwr16_and_fp64_query(cuda, Nx, hwr):
+    """The benchmark's h_w (16 lattice spacings) through queryVorticityAbs's
+    replacement, in FP32 (1e-5 of the field's scale) and in FP64 (1e-12)."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    prm, pos, om = _tg(Nx, hwr)
+    pts = (np.random.default_rng(Nx + 1).random((2000, 2)) * 1.2 - 0.1).astype(np.float32)
+    # the points wrapped into the domain in FP32, as the library wraps them
+    one = np.float32(1.0)
+    pw = (pts - np.floor(pts / one) * one).astype(np.float32)
+    dp, do, dq = to_dev(pos, cuda), to_dev(om, cuda), to_dev(pts, cuda)
+    for sign, us in ((1, False), (-1, True), (0, True)):
+        sel = om > 0 if sign > 0 else (om < 0 if sign < 0 else np.ones(len(om), bool))
+        w = om[sel] if us else np.abs(om[sel])
+        want = O.field_tiled_f64(pos[sel], w, pw, prm.h_w)
+        got = P.query_vorticity(dp, do, dq, sign=sign, use_signed=us, h_w=prm.h_w).cpu().numpy()
+        assert _rel(got, want) < 1e-5, (sign, us, _rel(got, want))
+        got64 = P.query_vorticity_f64(dp, do, dq, sign=sign, use_signed=us, h_w=prm.h_w).cpu().numpy()
+        assert _rel(got64, want) < 1e-12, (sign, us, _rel(got64, want))
+
+
 def test_query_random_particles_nonperiodic_and_exclude_center(cuda):
     from vortexparticlemc_cuda_gb300 import phash as P
     rng = np.random.default_rng(11)

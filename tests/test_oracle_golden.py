@@ -108,3 +108,41 @@ def test_reference_shim_agrees_when_present(golden):
     g = {key[len("hash1_"):]: golden[key] for key in golden.files if key.startswith("hash1_")}
     cn, ca, vc = O.ref_fill_cells(int(g["rshx"]), int(g["rshy"]), 1.0, 1.0, g["sub"], g["px"], g["py"])
     assert np.array_equal(vc, g["vp_cell"]) and np.array_equal(ca, g["cell_acc"])
+
+
+def test_omp_hash_pair_restatement(golden):
+    """FillCells_omp / CountingSort_omp (src/omp/hash_omp.cpp:12-70), restated
+    for the timed CPU baseline: the fill equals FillCells_cpu's golden output
+    at any thread count; with one thread the sort is the reference's formula
+    with its previous-cell base (hash_omp.cpp:65) -- wrong wherever a cell has
+    a non-empty predecessor -- and, where the reference's own build exists,
+    identical to it."""
+    g = {key[len("hash0_"):]: golden[key] for key in golden.files if key.startswith("hash0_")}
+    rx, ry = int(g["rshx"]), int(g["rshy"])
+    for nt in (1, 4):
+        cn, ca, vc, used = O.fill_cells_omp(rx, ry, float(g["Lx"]), float(g["Ly"]), g["sub"], g["px"], g["py"], nt)
+        assert used >= 1
+        assert np.array_equal(cn, g["cell_num_fill"]) and np.array_equal(ca, g["cell_acc"])
+        assert np.array_equal(vc, g["vp_cell"])
+    cn, ca, vc, _ = O.fill_cells_omp(rx, ry, float(g["Lx"]), float(g["Ly"]), g["sub"], g["px"], g["py"], 1)
+    cn2, vs, _ = O.counting_sort_omp(cn, ca, vc, 1)
+    want = np.zeros(len(vc), np.int32)
+    left = cn.copy()
+    for i in range(len(vc) - 1, -1, -1):
+        c = vc[i]
+        base = 0 if c == 0 else ca[c - 1]
+        want[left[c] - 1 + base] = i
+        left[c] -= 1
+    assert np.array_equal(vs, want) and not cn2.any()
+    assert not np.array_equal(vs, g["vp_sort"])            # the reference's OMP sort is incorrect
+    if O.ref_available():
+        import ctypes
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(1)
+        try:
+            rcn, rca, rvc = O.ref_fill_cells(rx, ry, float(g["Lx"]), float(g["Ly"]), g["sub"], g["px"], g["py"],
+                                              omp=True)
+            assert np.array_equal(rcn, cn) and np.array_equal(rca, ca) and np.array_equal(rvc, vc)
+            _, rvs = O.ref_counting_sort(rcn, rca, rvc, omp=True)
+            assert np.array_equal(rvs, vs)
+        finally:
+            ctypes.CDLL("libgomp.so.1").omp_set_num_threads(0 or __import__("os").cpu_count() or 1)

@@ -62,12 +62,15 @@ SIGNATURES = {
     "vpmc_kernel_icdf_table": (_i, [_f, _i, _vp, _vp]),
     "vpmc_cubic_spline": (_f, [_f, _f]),
     "vpmc_query_vorticity": (_i, [_vp, _i, _vp, _vp, _vp, _i, _vp, _i, _i, _i, _f, _f, _f, _i, _vp]),
+    "vpmc_query_vorticity_f64": (_i, [_vp, _i, _vp, _vp, _i, _vp, _i, _i, _f, _f, _f, _i, _vp]),
     "vpmc_rbf_matvec": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _i]),
     "vpmc_cg_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_cg_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_minres_rbf": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_minres_rbf_f64rhs": (_i, [_vp, _i, _vp, _vp, _vp, _f, _f, _f, _i, _d, _i, _vp]),
     "vpmc_sim_set_rbf_solver": (_i, [_vp, _i]),
+    "vpmc_sim_set_target_range": (_i, [_vp, C.c_longlong, C.c_longlong]),
+    "vpmc_sim_get_target_range": (_i, [_vp, _vp, _vp]),
     "vpmc_direct_velocity_f64": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _d, _i, _vp]),
     "vpmc_direct_velocity_f32": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _vp, _f, _f, _f, _i, _vp]),
     "vpmc_sim_create": (_i, [_vp, _i, _vp, _vp, C.POINTER(_vp)]),

@@ -328,6 +328,7 @@ extern "C" {
 int vpmc_sim_record(vpmc_sim* s, int nsteps, int k_ckpt) {
     if (!s || nsteps < 1 || k_ckpt < 1) return VPMC_ERR_INVALID;
     if (s->deform) return VPMC_ERR_UNSUPPORTED;   // the adjoint covers the plain method
+    if (s->t_begin != 0 || s->t_end != s->N) return VPMC_ERR_UNSUPPORTED;   // and whole simulations, not shards
     VPMC_CUDA(cudaSetDevice(s->ctx->device));
     if (!s->prepared) VPMC_TRY(vpmc_sim_prepare(s));
     cudaStream_t st = s->ctx->stream;
@@ -351,7 +352,7 @@ int vpmc_sim_record(vpmc_sim* s, int nsteps, int k_ckpt) {
 int vpmc_sim_adjoint(vpmc_sim* s, const double* dL_dXT, double* dL_dX0, double* dL_domega, int flags) {
     if (!s || !dL_dXT || !dL_dX0 || !dL_domega) return VPMC_ERR_INVALID;
     if (s->rec_steps < 1) return VPMC_ERR_INVALID;   // vpmc_sim_record first
-    if (s->deform) return VPMC_ERR_UNSUPPORTED;
+    if (s->deform || s->t_begin != 0 || s->t_end != s->N) return VPMC_ERR_UNSUPPORTED;
     vpmc_context* ctx = s->ctx;
     VPMC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;

@@ -491,14 +491,26 @@ __global__ void __launch_bounds__(kAsmThreads, 2) k_scatter_assemble(const uint4
             // inside each bin the records are ordered by sub-cell, so that
             // consecutive queries of a bin lie close together
             uint32_t kr[kPer];   // bin in the window | sub-cell << 8 | rank within (sub-cell, bin) << 12
+            const uint32_t lane = threadIdx.x & 31u;
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
                 const uint32_t k = threadIdx.x + uint32_t(j) * uint32_t(kAsmThreads);
-                if (k >= nw) break;
+                const bool valid = k < nw;
+                const unsigned vm = __ballot_sync(0xffffffffu, valid);
+                if (!valid) continue;
                 const uint32_t bl = r[j].w - uint32_t(b0);
                 const QRec q = make_qrec(r[j], inst, n_inst);
                 const uint32_t key = subcell_key(q.x, q.y, corg[bl]);
-                kr[j] = bl | (key << 8) | (atomicAdd(&sub[key * nb + bl], 1u) << 12);
+                // a window has few (sub-cell, bin) counters: lanes with the same one
+                // take their ranks from a single shared-memory atomic
+                const uint32_t ci = key * nb + bl;
+                const unsigned same = __match_any_sync(vm, ci);
+                const uint32_t leader = uint32_t(__ffs(same) - 1);
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(&sub[ci], uint32_t(__popc(same)));
+                base = __shfl_sync(same, base, int(leader));
+                const uint32_t rank = base + uint32_t(__popc(same & ((1u << lane) - 1u)));
+                kr[j] = bl | (key << 8) | (rank << 12);
                 r[j] = make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), q.id, q.flags);
             }
             __syncthreads();

@@ -273,7 +273,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // The same over aligned groups of G lanes (G a power of two <= 32); every lane
 // of the warp must take part.
 template <int G>
-__device__ __forceinline__ float group_sum_comp(float s, float c) {
+__device__ __forceinline__ void group_sum_comp_pair(float& s, float& c) {
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
         const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
@@ -284,20 +284,23 @@ __device__ __forceinline__ float group_sum_comp(float s, float c) {
         c = (lo ? c + c2 : c2 + c) - e;
         s = t;
     }
+}
+template <int G>
+__device__ __forceinline__ float group_sum_comp(float s, float c) {
+    group_sum_comp_pair<G>(s, c);
     return s - c;
 }
+// (sa - ca) - (sb - cb) of two compensated sums, the difference of the
+// leading parts taken exactly: no cancellation error when the two sums are
+// large and nearly equal (the two sign estimates of a velocity).
+__device__ __forceinline__ float comp_diff(float sa, float ca, float sb, float cb) {
+    float d, e;
+    two_sum(sa, -sb, d, e);
+    return d + (e - (ca - cb));
+}
 __device__ __forceinline__ float warp_sum_comp(float s, float c) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
-        const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
-        float t, e;
-        // order-independent pairing: combine (min lane, max lane) consistently
-        const bool lo = (threadIdx.x & o) == 0;
-        two_sum(lo ? s : s2, lo ? s2 : s, t, e);
-        c = (lo ? c + c2 : c2 + c) - e;
-        s = t;
-    }
+    // order-independent pairing: combine (min lane, max lane) consistently
+    group_sum_comp_pair<32>(s, c);
     return s - c;
 }
 

@@ -197,6 +197,31 @@ int vpmc_query_vorticity(vpmc_context* ctx, int N, const float* pos, const float
     return vpmc_context_sync(ctx);
 }
 
+int vpmc_query_vorticity_f64(vpmc_context* ctx, int N, const float* pos, const float* omega, int M, const float* pts,
+                             int sign, int use_signed, float h_w, float Lx, float Ly, int periodic, double* out) {
+    if (!ctx || N < 0 || M < 0 || !(h_w > 0.f) || !(Lx > 0.f) || !(Ly > 0.f)) return VPMC_ERR_INVALID;
+    if ((N > 0 && (!pos || !omega)) || (M > 0 && (!pts || !out))) return VPMC_ERR_INVALID;
+    VPMC_CUDA(cudaSetDevice(ctx->device));
+    if (M == 0) return VPMC_OK;
+    cudaStream_t st = ctx->stream;
+    VPMC_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * size_t(M), st));
+    if (N == 0) return vpmc_context_sync(ctx);
+    Work w;
+    VPMC_TRY(setup(ctx, SLOT_QUERY, N, h_w, Lx, Ly, periodic, M, 0, &w));
+    const int set_mode = sign > 0 ? SET_POS_ONLY
+                                   : (sign < 0 ? SET_NEG_ONLY : (use_signed ? SET_ONE_SIGNED : SET_ONE_ABS));
+    VPMC_TRY(grid_build(ctx, w.g, reinterpret_cast<const float2*>(pos), omega, set_mode));
+    VPMC_TRY(bin_points(ctx, w.g, w.q, reinterpret_cast<const float2*>(pts), M, 0, 0));
+    VPMC_TRY(make_items(ctx, w.g, w.q.qstart, w.it, query_chunk(4)));
+    EvalLaunch L;
+    L.mode = EVAL_FIELD64;
+    L.out_f64 = out;
+    VPMC_TRY(launch_eval(ctx, w.g, w.q.qrec, w.it, L));
+    if (sign < 0 && use_signed)
+        VPMC_LAUNCH(k_axpby, blocks_for(M), 256, 0, st, out, out, long(M), -1.0, 0.0, out);
+    return vpmc_context_sync(ctx);
+}
+
 int vpmc_rbf_matvec(vpmc_context* ctx, int N, const float* pos, const float* x, float* y, float h_w, float Lx,
                     float Ly, int periodic, int precise) {
     if (!ctx || N < 0 || !(h_w > 0.f) || !(Lx > 0.f) || !(Ly > 0.f)) return VPMC_ERR_INVALID;

@@ -326,10 +326,25 @@ __device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f,
     return make_float2(-ry * sc, rx * sc);
 }
 
-// Plain method: 8 lanes per target, 4 targets per warp.  Each lane sums its
-// samples j = l, l + 8, ... (four loads in flight before their terms are
-// added), then the 8 lanes combine their compensated sums in a fixed tree.
+// Plain method: 8 lanes per target, 4 targets per warp.  With an even
+// sample count per sign, lane l sums the sample pairs (j, j + 1),
+// j = 2 l + 16 v: one 16-byte point load and one 8-byte field load per pair,
+// 128-byte contiguous runs per 8-lane group, and the next two pairs' loads
+// issued before the current two are summed; otherwise single samples
+// j = l + 8 v.  The 8 lanes then combine their compensated sums in a fixed tree.
 constexpr int kAccLanes = 8;
+
+__device__ __forceinline__ void acc_pair_load(const float2* ys, const float* fv, long base, int j, int Q, bool live,
+                                              float4& y, float2& f) {
+    if (live && j < Q) {
+        y = __ldg(reinterpret_cast<const float4*>(ys + base + j));
+        f = __ldg(reinterpret_cast<const float2*>(fv + base + j));
+    } else {
+        y = make_float4(0.f, 0.f, 0.f, 0.f);
+        f = make_float2(0.f, 0.f);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
     const int lane = threadIdx.x & 31, sub = lane & (kAccLanes - 1), grp = lane / kAccLanes;
     constexpr int kPerWarp = 32 / kAccLanes;
@@ -347,32 +362,68 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
         const float2 x = a.pos[t];
         const float R = disk_radius(x, I.periodic != 0, I.Lx, I.Ly);
         const float alpha = 1.f / (2.f * kPiF * R);
-        float u[2][2];
+        float u[2][2], uc[2][2];
         for (int s = 0; s < 2; ++s) {
             KSum sx, sy;
             const long base = (tl * 2 + s) * Q;
-            for (int j0 = sub; j0 < Q; j0 += 4 * kAccLanes) {
-                float2 y[4];
-                float f[4];
+            if ((Q & 1) == 0) {
+                constexpr int kStep = 2 * kAccLanes;   // samples a group covers per pair load
+                int j = 2 * sub;
+                float4 ya, yb;
+                float2 fa, fb;
+                acc_pair_load(a.ys, a.fv, base, j, Q, live, ya, fa);
+                acc_pair_load(a.ys, a.fv, base, j + kStep, Q, live, yb, fb);
+                for (; j < Q; j += 2 * kStep) {
+                    float4 yc, yd;
+                    float2 fc, fd;
+                    acc_pair_load(a.ys, a.fv, base, j + 2 * kStep, Q, live, yc, fc);
+                    acc_pair_load(a.ys, a.fv, base, j + 3 * kStep, Q, live, yd, fd);
+                    const float2 ys4[4] = {make_float2(ya.x, ya.y), make_float2(ya.z, ya.w), make_float2(yb.x, yb.y),
+                                           make_float2(yb.z, yb.w)};
+                    const float fs4[4] = {fa.x, fa.y, fb.x, fb.y};
 #pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    const int j = j0 + kAccLanes * v;
-                    y[v] = live && j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
-                    f[v] = live && j < Q ? a.fv[base + j] : 0.f;
+                    for (int v = 0; v < 4; ++v) {
+                        if (j + (v >> 1) * kStep >= Q) break;
+                        const float2 c = mis_term(I.law, x, ys4[v], fs4[v], w1, w2, I.cum9[s], alpha, R, I);
+                        sx.add(c.x);
+                        sy.add(c.y);
+                    }
+                    ya = yc;
+                    yb = yd;
+                    fa = fc;
+                    fb = fd;
                 }
+            } else {
+                for (int j0 = sub; j0 < Q; j0 += 4 * kAccLanes) {
+                    float2 y[4];
+                    float f[4];
 #pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    if (j0 + kAccLanes * v >= Q) break;
-                    const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
-                    sx.add(c.x);
-                    sy.add(c.y);
+                    for (int v = 0; v < 4; ++v) {
+                        const int j = j0 + kAccLanes * v;
+                        y[v] = live && j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
+                        f[v] = live && j < Q ? a.fv[base + j] : 0.f;
+                    }
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        if (j0 + kAccLanes * v >= Q) break;
+                        const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
+                        sx.add(c.x);
+                        sy.add(c.y);
+                    }
                 }
             }
-            u[s][0] = group_sum_comp<kAccLanes>(sx.s, sx.c) * inv;
-            u[s][1] = group_sum_comp<kAccLanes>(sy.s, sy.c) * inv;
+            group_sum_comp_pair<kAccLanes>(sx.s, sx.c);
+            group_sum_comp_pair<kAccLanes>(sy.s, sy.c);
+            u[s][0] = sx.s;
+            u[s][1] = sy.s;
+            uc[s][0] = sx.c;
+            uc[s][1] = sy.c;
         }
         if (live && sub == 0) {
-            const float vx = u[0][0] - u[1][0], vy = u[0][1] - u[1][1];
+            // u(+) - u(-) with the leading parts subtracted exactly: a near-singular
+            // sample makes both sign sums large, their difference small
+            const float vx = comp_diff(u[0][0], uc[0][0], u[1][0], uc[1][0]) * inv;
+            const float vy = comp_diff(u[0][1], uc[0][1], u[1][1], uc[1][1]) * inv;
             a.vel[t] = make_float2(vx, vy);
             if (a.advect) {
                 double nx = double(x.x) + double(I.dt) * double(vx);
@@ -436,9 +487,7 @@ __global__ void __launch_bounds__(256) k_accum5(Acc5Args a) {
             R[k] = disk_radius(xa[k], I.periodic != 0, I.Lx, I.Ly);
             alpha[k] = 1.f / (2.f * kPiF * R[k]);
         }
-        float u[5][2];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) u[k][0] = u[k][1] = 0.f;
+        float u[5][2], su[2][5][2], cu[2][5][2];
         for (int s = 0; s < 2; ++s) {
             KSum sx[5], sy[5];
             const long base = (tl * 2 + s) * Q;
@@ -462,13 +511,20 @@ __global__ void __launch_bounds__(256) k_accum5(Acc5Args a) {
                     sy[k].add(c.y);
                 }
             }
-            const float sg = s == 0 ? 1.f : -1.f;
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                u[k][0] += sg * (warp_sum_comp(sx[k].s, sx[k].c) * inv);
-                u[k][1] += sg * (warp_sum_comp(sy[k].s, sy[k].c) * inv);
+                group_sum_comp_pair<32>(sx[k].s, sx[k].c);
+                group_sum_comp_pair<32>(sy[k].s, sy[k].c);
+                su[s][k][0] = sx[k].s;
+                cu[s][k][0] = sx[k].c;
+                su[s][k][1] = sy[k].s;
+                cu[s][k][1] = sy[k].c;
             }
         }
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) u[k][d] = comp_diff(su[0][k][d], cu[0][k][d], su[1][k][d], cu[1][k][d]) * inv;
         if (lane == 0) {
             const float vx = u[0][0], vy = u[0][1];
             a.vel[t] = make_float2(vx, vy);
@@ -806,8 +862,8 @@ int refresh_cover(vpmc_sim* s, bool from_step, bool reset, bool realloc = false)
 
 // The sample buffer holds the last chunk's samples after a pass.
 void mark_samples(vpmc_sim* s) {
-    s->ys_t0 = ((s->N - 1) / s->chunk_targets) * s->chunk_targets;
-    s->ys_nt = s->N - s->ys_t0;
+    s->ys_t0 = s->t_begin + ((s->t_end - s->t_begin - 1) / s->chunk_targets) * s->chunk_targets;
+    s->ys_nt = s->t_end - s->ys_t0;
 }
 
 // Issue one MIS pass over all targets (advect: positions -> pos_next, then
@@ -827,8 +883,8 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     const long Q = samples_per(s);
     if (!def) VPMC_LAUNCH(k_sub_pos, blocks_for(2 * s->N), 256, 0, st, s->d_mc, s->n_inst, s->sub, s->pos, 2 * s->N,
                           s->pos_sub);
-    for (long t0 = 0; t0 < s->N; t0 += s->chunk_targets) {
-        const long nt = std::min(s->chunk_targets, s->N - t0);
+    for (long t0 = s->t_begin; t0 < s->t_end; t0 += s->chunk_targets) {
+        const long nt = std::min(s->chunk_targets, s->t_end - t0);
         const long ns = nt * 2 * Q;
         VPMC_CUDA(cudaMemsetAsync(s->q.qcount, 0, sizeof(uint32_t) * size_t(s->g.nbins + 1), st));
         GenArgs ga{s->d_mc, s->n_inst, s->g.inst, s->pos, def ? s->F : nullptr, def ? nullptr : s->pos_sub, s->sub,
@@ -848,7 +904,7 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
         L.qpt = f64 ? 4 : s->qpt;
         L.out_f32 = s->fv;
         L.out_f64 = s->fv64;
-        const size_t ci = size_t(t0 / s->chunk_targets);
+        const size_t ci = size_t((t0 - s->t_begin) / s->chunk_targets);
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci], st, ev_flags));
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
         if (timed) VPMC_CUDA(cudaEventRecordWithFlags(s->chunk_ev[2 * ci + 1], st, ev_flags));
@@ -868,9 +924,11 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
     }
     mark_samples(s);
     if (advect) {
-        VPMC_CUDA(cudaMemcpyAsync(s->pos, s->pos_next, sizeof(float2) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+        // only the pass's targets moved (a shard leaves the others to the exchange)
+        const size_t tb = size_t(s->t_begin), tn = size_t(s->t_end - s->t_begin);
+        VPMC_CUDA(cudaMemcpyAsync(s->pos + tb, s->pos_next + tb, sizeof(float2) * tn, cudaMemcpyDeviceToDevice, st));
         if (def)
-            VPMC_CUDA(cudaMemcpyAsync(s->F, s->F_next, sizeof(float4) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
+            VPMC_CUDA(cudaMemcpyAsync(s->F + tb, s->F_next + tb, sizeof(float4) * tn, cudaMemcpyDeviceToDevice, st));
         VPMC_LAUNCH(k_inc_step, 1, 1, 0, st, s->d_step);
     }
     *nlaunch = int(vpmc_kernel_launch_count() - l0);
@@ -879,7 +937,7 @@ int issue_pass(vpmc_sim* s, bool advect, bool timed, int* nlaunch) {
 
 // Device time of the eval launches of the last completed pass (call after a sync).
 int collect_eval_time(vpmc_sim* s) {
-    const long nchunks = (s->N + s->chunk_targets - 1) / s->chunk_targets;
+    const long nchunks = (s->t_end - s->t_begin + s->chunk_targets - 1) / s->chunk_targets;
     float tot = 0.f;
     for (long c = 0; c < nchunks; ++c) {
         float ms = 0.f;
@@ -968,6 +1026,8 @@ int vpmc_sim_create(vpmc_context* ctx, int n_inst, const vpmc_sim_params* prms, 
     s->counts.assign(counts, counts + n_inst);
     s->begin.resize(n_inst);
     s->N = N;
+    s->t_begin = 0;
+    s->t_end = N;
     s->N1 = prms[0].N1;
     s->N2 = prms[0].N2;
     s->max_samples = 1L << 30;   // samples per chunk (~52 B of records each): fuller bins, fewer passes
@@ -1266,6 +1326,24 @@ int vpmc_sim_set_precision(vpmc_sim* s, int bits) {
     return vpmc_context_sync(s->ctx);
 }
 
+int vpmc_sim_set_target_range(vpmc_sim* s, long long begin, long long end) {
+    if (!s || begin < 0 || end > s->N || begin >= end) return VPMC_ERR_INVALID;
+    if (s->deform && (begin != 0 || end != s->N)) return VPMC_ERR_UNSUPPORTED;
+    s->t_begin = long(begin);
+    s->t_end = long(end);
+    s->ys_t0 = -1;
+    s->ys_nt = 0;
+    drop_graphs(s);   // the captured passes cover the old range (the chunk events cover all N)
+    return VPMC_OK;
+}
+
+int vpmc_sim_get_target_range(vpmc_sim* s, long long* begin, long long* end) {
+    if (!s) return VPMC_ERR_INVALID;
+    if (begin) *begin = s->t_begin;
+    if (end) *end = s->t_end;
+    return VPMC_OK;
+}
+
 int vpmc_sim_set_rbf_solver(vpmc_sim* s, int solver) {
     if (!s || (solver != VPMC_RBF_CG && solver != VPMC_RBF_MINRES)) return VPMC_ERR_INVALID;
     s->rbf_solver = solver;
@@ -1404,7 +1482,7 @@ int vpmc_sim_geometry(vpmc_sim* s, long long* info) {
     if (!s || !info) return VPMC_ERR_INVALID;
     info[0] = s->N;
     info[1] = s->chunk_targets;
-    info[2] = (s->N + s->chunk_targets - 1) / s->chunk_targets;
+    info[2] = (s->t_end - s->t_begin + s->chunk_targets - 1) / s->chunk_targets;
     info[3] = s->g.nbins;
     info[4] = s->plan.empty() ? 0 : s->plan[0].gx;
     info[5] = s->plan.empty() ? 0 : s->plan[0].k;
@@ -1502,6 +1580,7 @@ int vpmc_sim_freeze_sampling(vpmc_sim* s, int on) {
 int vpmc_sim_set_deformation(vpmc_sim* s, int on, float min_cover) {
     if (!s || !(min_cover <= kCoverCap)) return VPMC_ERR_INVALID;
     if (on && s->precision == 64) return VPMC_ERR_UNSUPPORTED;
+    if (on && (s->t_begin != 0 || s->t_end != s->N)) return VPMC_ERR_UNSUPPORTED;   // no F exchange for shards
     VPMC_CUDA(cudaSetDevice(s->ctx->device));
     if (on && !s->vel5) {
         VPMC_TRY(s->aux.reserve(5 * sizeof(float2) * size_t(s->N)));

@@ -95,6 +95,7 @@ struct vpmc_sim {
     std::vector<int> counts;
     std::vector<long> begin;
     long N = 0;
+    long t_begin = 0, t_end = 0;       // targets a pass estimates and advects (a shard); all N by default
     int N1 = 0, N2 = 0;
     uint64_t step = 0;
     int k_walk = 0, qpt = 4;

@@ -21,7 +21,7 @@ from ._lib import (DIRECT_MOLLIFIED, DIRECT_PLUMMER, LAW_REFERENCE, LAW_UNBIASED
 
 __all__ = [
     "fill_dummy", "Context", "context", "fill_cells", "counting_sort", "hash_build", "build_subsets",
-    "kernel_icdf_table", "cubic_spline", "query_vorticity", "rbf_matvec", "cg_rbf", "minres_rbf", "direct_velocity",
+    "kernel_icdf_table", "cubic_spline", "query_vorticity", "query_vorticity_f64", "rbf_matvec", "cg_rbf", "minres_rbf", "direct_velocity",
     "Simulation", "SimParam", "philox4x32_10", "launch_count", "LAW_REFERENCE", "LAW_UNBIASED",
     "DIRECT_MOLLIFIED", "DIRECT_PLUMMER", "RBF_CG", "RBF_MINRES",
 ]
@@ -197,6 +197,18 @@ def query_vorticity(pos, omega, pts, sign=1, use_signed=False, exclude_center=Fa
     return out
 
 
+def query_vorticity_f64(pos, omega, pts, sign=1, use_signed=False, h_w=0.04, Lx=1.0, Ly=1.0, periodic=True):
+    """The vorticity query with every pair and the sum in FP64 -> (M,) float64."""
+    pos = _cuda(pos, torch.float32, "pos", (2,))
+    omega = _cuda(omega, torch.float32, "omega")
+    pts = _cuda(pts, torch.float32, "pts", (2,))
+    out = torch.empty(pts.shape[0], dtype=torch.float64, device=pts.device)
+    check(lib().vpmc_query_vorticity_f64(context(_dev(pos)).h, pos.shape[0], _p(pos), _p(omega), pts.shape[0],
+                                         _p(pts), int(sign), int(use_signed), h_w, Lx, Ly, int(periodic), _p(out)),
+          "vpmc_query_vorticity_f64")
+    return out
+
+
 # ---------------------------------------------------------------- RBF / CG (a10)
 def rbf_matvec(pos, x, h_w, Lx=1.0, Ly=1.0, periodic=True, precise=True):
     """Ax_cuda (src/cuda/cg_rbf_init.cu:33-50)."""
@@ -367,6 +379,21 @@ class Simulation:
             check(st, "vpmc_sim_init_strengths")
         return [dict(iters=int(info[3 * i]), relres=info[3 * i + 1], true_relres=info[3 * i + 2])
                 for i in range(len(self.counts))]
+
+    def set_target_range(self, begin: int, end: int):
+        """Estimate and advect only particles [begin, end) (a shard); all stay sources."""
+        check(lib().vpmc_sim_set_target_range(self.h, int(begin), int(end)), "vpmc_sim_set_target_range")
+
+    def target_range(self):
+        b, e = C.c_longlong(), C.c_longlong()
+        check(lib().vpmc_sim_get_target_range(self.h, C.byref(b), C.byref(e)), "vpmc_sim_get_target_range")
+        return b.value, e.value
+
+    def positions_into(self, out):
+        """Copy the positions into `out`, an (N, 2) float32 CUDA tensor (no allocation)."""
+        out = _cuda(out, torch.float32, "out", (2,))
+        check(lib().vpmc_sim_get_particles(self.h, _p(out), None, None, 0), "vpmc_sim_get_particles")
+        return out
 
     def set_rbf_solver(self, solver: int):
         """RBF_CG (the reference's conjugate_gradient_rbf) or RBF_MINRES for
