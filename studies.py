@@ -293,6 +293,18 @@ def study_error_cost(args):
             truth = P.direct_velocity(p, om, P.DIRECT_MOLLIFIED, pts=p[tsel], param=h_w).cpu().numpy()
         v = sim.velocity(step=0)[tsel].cpu().numpy()
         err = rel_rms(v, truth)
+        fp64 = {}
+        if n == 64 and args.fp64:
+            # the FP64 path at the same positions and step (same samples)
+            sim.set_precision(64)
+            sim.set_tuning(4, 4)
+            t0 = time.perf_counter()
+            v64 = sim.velocity(step=0)[tsel].cpu().numpy()
+            fp64 = {"fp64_path_pass_s": time.perf_counter() - t0,
+                    "fp64_vel_rel_rms_vs_fp64_direct": rel_rms(v64, truth),
+                    "fp32_vs_fp64_path_same_samples": rel_rms(v, v64)}
+            sim.set_precision(32)
+            sim.set_tuning(7, 4)
         sim.set_step(0)
         sim.step(3, use_graph=True)               # warm-up (graph capture)
         torch.cuda.synchronize(dev)
@@ -305,15 +317,7 @@ def study_error_cost(args):
         torch.cuda.synchronize(dev)
         ms = s.elapsed_time(e) / steps
         row = {"N1=N2": n, "vel_rel_rms_vs_fp64_direct": err, "ms_per_step": ms,
-               "particle_steps_per_s": len(pos) / (ms / 1e3), "eval_ms": sim.last_stats()["eval_ms"]}
-        if n == 64 and args.fp64:
-            sim.set_precision(64)
-            sim.set_tuning(4, 4)
-            t0 = time.perf_counter()
-            v64 = sim.velocity(step=0)[tsel].cpu().numpy()
-            row["fp64_path_pass_s"] = time.perf_counter() - t0
-            row["fp64_vel_rel_rms_vs_fp64_direct"] = rel_rms(v64, truth)
-            row["fp32_vs_fp64_path_same_samples"] = rel_rms(v, v64)
+               "particle_steps_per_s": len(pos) / (ms / 1e3), "eval_ms": sim.last_stats()["eval_ms"], **fp64}
         log(f"{row}")
         rows.append(row)
         sim.close()

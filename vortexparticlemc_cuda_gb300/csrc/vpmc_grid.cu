@@ -491,26 +491,14 @@ __global__ void __launch_bounds__(kAsmThreads, 2) k_scatter_assemble(const uint4
             // inside each bin the records are ordered by sub-cell, so that
             // consecutive queries of a bin lie close together
             uint32_t kr[kPer];   // bin in the window | sub-cell << 8 | rank within (sub-cell, bin) << 12
-            const uint32_t lane = threadIdx.x & 31u;
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
                 const uint32_t k = threadIdx.x + uint32_t(j) * uint32_t(kAsmThreads);
-                const bool valid = k < nw;
-                const unsigned vm = __ballot_sync(0xffffffffu, valid);
-                if (!valid) continue;
+                if (k >= nw) break;
                 const uint32_t bl = r[j].w - uint32_t(b0);
                 const QRec q = make_qrec(r[j], inst, n_inst);
                 const uint32_t key = subcell_key(q.x, q.y, corg[bl]);
-                // a window has few (sub-cell, bin) counters: lanes with the same one
-                // take their ranks from a single shared-memory atomic
-                const uint32_t ci = key * nb + bl;
-                const unsigned same = __match_any_sync(vm, ci);
-                const uint32_t leader = uint32_t(__ffs(same) - 1);
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&sub[ci], uint32_t(__popc(same)));
-                base = __shfl_sync(same, base, int(leader));
-                const uint32_t rank = base + uint32_t(__popc(same & ((1u << lane) - 1u)));
-                kr[j] = bl | (key << 8) | (rank << 12);
+                kr[j] = bl | (key << 8) | (atomicAdd(&sub[key * nb + bl], 1u) << 12);
                 r[j] = make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), q.id, q.flags);
             }
             __syncthreads();
@@ -741,7 +729,6 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     __shared__ Piece s_pc[kMaxPieces];
     __shared__ BatchPiece s_bp[kMaxPieces + 2];
     __shared__ uint2 s_rng[kEvalThreads / 32][kMaxPieces + 2];   // per warp: its part of each batch piece
-    __shared__ uint32_t s_coff[kMaxPieces + 2];                   // packed offset of each piece's part
     __shared__ float4 s_wb[kEvalThreads / 32];                    // per warp: query bounding box (x0, x1, y0, y1)
     __shared__ int s_np, s_nbp, s_cur_piece, s_abort, s_pre;
     __shared__ uint32_t s_cur_off, s_btot, s_item;
@@ -1040,75 +1027,37 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             const int nbp = s_nbp;
             if constexpr (kPacked) {
                 // staged candidates -> image-shifted, bin-local coordinates + kappa c2
-                // (kappa = -3/h^2 scales every squared distance, see packed_run),
-                // keeping only this warp's part of each run and packing those parts
-                // to the front of the staging buffer in run order, so that a sweep
-                // is one contiguous loop.  In place: a record's packed slot never
-                // lies past its staged slot, and every lane reads its record before
-                // any lane writes (the warp is the CTA).
+                // (kappa = -3/h^2 scales every squared distance, see packed_run)
                 const float kap = G.B;
-                const int wid = tid >> 5, lane = tid & 31;
-                if (npw > 0) {
-                    uint32_t k0 = 0u, k1 = 0u;   // kept records of runs lane and lane + 32
-                    if (lane < nbp) k0 = s_rng[wid][lane].y - s_rng[wid][lane].x;
-                    if (lane + 32 < nbp) k1 = s_rng[wid][lane + 32].y - s_rng[wid][lane + 32].x;
-                    uint32_t i0 = k0, i1 = k1;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y0 = __shfl_up_sync(0xffffffffu, i0, o);
-                        const uint32_t y1 = __shfl_up_sync(0xffffffffu, i1, o);
-                        if (lane >= o) { i0 += y0; i1 += y1; }
-                    }
-                    const uint32_t tot0 = __shfl_sync(0xffffffffu, i0, 31);
-                    if (lane < nbp) s_coff[lane] = i0 - k0;
-                    if (lane + 32 < nbp) s_coff[lane + 32] = tot0 + i1 - k1;
-                    __syncwarp();
-                    for (int b = 0; b < nbp; ++b) {
-                        const BatchPiece bp = s_bp[b];
-                        const Piece pc = s_pc[bp.piece];
-                        const uint2 rg = s_rng[wid][b];
-                        const uint32_t n = rg.y - rg.x, dst = s_coff[b], src = bp.soff + rg.x;
-                        const float ox = s_ox + pc.qdx, oy = s_oy + pc.qdy;
-                        for (uint32_t c0 = 0; c0 < n; c0 += 32u) {
-                            const uint32_t c = c0 + uint32_t(lane);
-                            const bool v = c < n;
-                            if constexpr (kDef) {
-                                float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f), f1 = f0;
-                                if (v) {
-                                    const float4* r = reinterpret_cast<const float4*>(s_candf[src + c].f);
-                                    f0 = r[0];   // x, y, g11, g12
-                                    f1 = r[1];   // g22, w, wl, 0
-                                }
-                                __syncwarp();
-                                if (v) {
-                                    const float lx = f0.x - ox, ly = f0.y - oy;
-                                    const float g11 = f0.z, g12 = f0.w, g22 = f1.x, w = f1.y;
-                                    const float gx = fmaf(g11, lx, g12 * ly), gy = fmaf(g12, lx, g22 * ly);
-                                    const float e = kap * fmaf(lx, gx, ly * gy);
-                                    const float a11 = kap * g11, a12 = kap * (2.f * g12), a22 = kap * g22;
-                                    const float ax = kap * (-2.f * gx), ay = kap * (-2.f * gy);
-                                    float4* d = reinterpret_cast<float4*>(s_candf[dst + c].f);
-                                    d[0] = make_float4(a11, a11, a12, a12);
-                                    d[1] = make_float4(a22, a22, ax, ax);
-                                    d[2] = make_float4(ay, ay, e, e);
-                                    d[3] = make_float4(w, w, 0.f, 0.f);
-                                }
-                            } else {
-                                float4 xy = make_float4(0.f, 0.f, 0.f, 0.f), ww = xy;
-                                if (v) {
-                                    const float4* r = reinterpret_cast<const float4*>(&s_cand[src + c]);
-                                    xy = r[0];   // x, x, y, y
-                                    ww = r[1];   // w, w, wl, pad
-                                }
-                                __syncwarp();
-                                if (v) {
-                                    const float lx = xy.x - ox, ly = xy.z - oy;
-                                    const float c2 = kap * fmaf(lx, lx, ly * ly);
-                                    float4* d = reinterpret_cast<float4*>(&s_cand[dst + c]);
-                                    d[0] = make_float4(lx, lx, ly, ly);
-                                    d[1] = make_float4(ww.x, ww.x, c2, c2);
-                                }
-                            }
+                for (int b = 0; b < nbp; ++b) {
+                    const BatchPiece bp = s_bp[b];
+                    const Piece pc = s_pc[bp.piece];
+                    const float ox = s_ox + pc.qdx, oy = s_oy + pc.qdy;
+                    for (uint32_t c = threadIdx.x; c < bp.cnt; c += kEvalThreads) {
+                        if constexpr (kDef) {
+                            float* f = s_candf[bp.soff + c].f;
+                            const float lx = f[0] - ox, ly = f[1] - oy;
+                            const float g11 = f[2], g12 = f[3], g22 = f[4], w = f[5];
+                            const float gx = fmaf(g11, lx, g12 * ly), gy = fmaf(g12, lx, g22 * ly);
+                            const float e = kap * fmaf(lx, gx, ly * gy);
+                            f[0] = kap * g11; f[1] = f[0];
+                            f[2] = kap * (2.f * g12); f[3] = f[2];
+                            f[4] = kap * g22; f[5] = f[4];
+                            f[6] = kap * (-2.f * gx); f[7] = f[6];
+                            f[8] = kap * (-2.f * gy); f[9] = f[8];
+                            f[10] = e; f[11] = e;
+                            f[12] = w; f[13] = w;
+                            f[14] = 0.f; f[15] = 0.f;
+                        } else {
+                            Cand& cd = s_cand[bp.soff + c];
+                            const float lx = cd.x - ox, ly = cd.y - oy;
+                            const float c2 = kap * fmaf(lx, lx, ly * ly);
+                            cd.x = lx;
+                            cd.x2 = lx;
+                            cd.y = ly;
+                            cd.y2 = ly;
+                            cd.wl = c2;
+                            cd.pad = c2;
                         }
                     }
                 }
@@ -1148,18 +1097,15 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         QY[pr] = pk2(ay, by);
                         P[pr] = pk2(0.f, 0.f);
                     }
-                    if (npw > 0) {
-                        // the sweep's packed records: runs bfirst..b, contiguous
-                        const uint2 rl = s_rng[tid >> 5][b];
-                        const uint32_t p0 = s_coff[bfirst], p1 = s_coff[b] + (rl.y - rl.x);
-                        const int n = int(p1 - p0);
-                        const CandF* csf = s_candf + p0;
-                        if (n > 0) {
-                            if (npw == 1) packed_run_f<1, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
-                            else if (NP >= 2 && npw == 2)
-                                packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
-                            else packed_run_f<NP, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
-                        }
+                    for (int gb = bfirst; gb <= b && npw > 0; ++gb) {
+                        const uint2 rg = s_rng[tid >> 5][gb];
+                        const int n = int(rg.y) - int(rg.x);
+                        if (n <= 0) continue;
+                        const CandF* csf = s_candf + s_bp[gb].soff + rg.x;
+                        if (npw == 1) packed_run_f<1, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
+                        else if (NP >= 2 && npw == 2)
+                            packed_run_f<(NP >= 2 ? 2 : 1), NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
+                        else packed_run_f<NP, NP>(csf, n, QXX, QXY, QYY, QX, QY, P);
                     }
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
@@ -1181,18 +1127,15 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         Q2[pr] = pk2(kap * fmaf(ax, ax, ay * ay), kap * fmaf(bx, bx, by * by));
                         P[pr] = pk2(0.f, 0.f);
                     }
-                    // a warp with few queries runs fewer pairs (none when it holds no
-                    // query); the sweep's packed records (runs bfirst..b) are contiguous
-                    if (npw > 0) {
-                        const uint2 rl = s_rng[tid >> 5][b];
-                        const uint32_t p0 = s_coff[bfirst], p1 = s_coff[b] + (rl.y - rl.x);
-                        const int n = int(p1 - p0);
-                        const Cand* c0 = s_cand + p0;
-                        if (n > 0) {
-                            if (npw == 1) packed_run<1, NP>(c0, n, QX, QY, Q2, P);
-                            else if (NP >= 2 && npw == 2) packed_run<(NP >= 2 ? 2 : 1), NP>(c0, n, QX, QY, Q2, P);
-                            else packed_run<NP, NP>(c0, n, QX, QY, Q2, P);
-                        }
+                    // a warp with few queries runs fewer pairs (none when it holds no query)
+                    for (int gb = bfirst; gb <= b && npw > 0; ++gb) {
+                        const uint2 rg = s_rng[tid >> 5][gb];
+                        const int n = int(rg.y) - int(rg.x);
+                        if (n <= 0) continue;
+                        const Cand* c0 = s_cand + s_bp[gb].soff + rg.x;
+                        if (npw == 1) packed_run<1, NP>(c0, n, QX, QY, Q2, P);
+                        else if (NP >= 2 && npw == 2) packed_run<(NP >= 2 ? 2 : 1), NP>(c0, n, QX, QY, Q2, P);
+                        else packed_run<NP, NP>(c0, n, QX, QY, Q2, P);
                     }
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {

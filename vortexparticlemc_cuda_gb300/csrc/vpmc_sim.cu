@@ -326,24 +326,10 @@ __device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f,
     return make_float2(-ry * sc, rx * sc);
 }
 
-// Plain method: 8 lanes per target, 4 targets per warp.  With an even
-// sample count per sign, lane l sums the sample pairs (j, j + 1),
-// j = 2 l + 16 v: one 16-byte point load and one 8-byte field load per pair,
-// 128-byte contiguous runs per 8-lane group, and the next two pairs' loads
-// issued before the current two are summed; otherwise single samples
-// j = l + 8 v.  The 8 lanes then combine their compensated sums in a fixed tree.
+// Plain method: 8 lanes per target, 4 targets per warp.  Each lane sums its
+// samples j = l, l + 8, ... (four loads in flight before their terms are
+// added), then the 8 lanes combine their compensated sums in a fixed tree.
 constexpr int kAccLanes = 8;
-
-__device__ __forceinline__ void acc_pair_load(const float2* ys, const float* fv, long base, int j, int Q, bool live,
-                                              float4& y, float2& f) {
-    if (live && j < Q) {
-        y = __ldg(reinterpret_cast<const float4*>(ys + base + j));
-        f = __ldg(reinterpret_cast<const float2*>(fv + base + j));
-    } else {
-        y = make_float4(0.f, 0.f, 0.f, 0.f);
-        f = make_float2(0.f, 0.f);
-    }
-}
 
 __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
     const int lane = threadIdx.x & 31, sub = lane & (kAccLanes - 1), grp = lane / kAccLanes;
@@ -366,50 +352,21 @@ __global__ void __launch_bounds__(256) k_accum(AccArgs a) {
         for (int s = 0; s < 2; ++s) {
             KSum sx, sy;
             const long base = (tl * 2 + s) * Q;
-            if ((Q & 1) == 0) {
-                constexpr int kStep = 2 * kAccLanes;   // samples a group covers per pair load
-                int j = 2 * sub;
-                float4 ya, yb;
-                float2 fa, fb;
-                acc_pair_load(a.ys, a.fv, base, j, Q, live, ya, fa);
-                acc_pair_load(a.ys, a.fv, base, j + kStep, Q, live, yb, fb);
-                for (; j < Q; j += 2 * kStep) {
-                    float4 yc, yd;
-                    float2 fc, fd;
-                    acc_pair_load(a.ys, a.fv, base, j + 2 * kStep, Q, live, yc, fc);
-                    acc_pair_load(a.ys, a.fv, base, j + 3 * kStep, Q, live, yd, fd);
-                    const float2 ys4[4] = {make_float2(ya.x, ya.y), make_float2(ya.z, ya.w), make_float2(yb.x, yb.y),
-                                           make_float2(yb.z, yb.w)};
-                    const float fs4[4] = {fa.x, fa.y, fb.x, fb.y};
+            for (int j0 = sub; j0 < Q; j0 += 4 * kAccLanes) {
+                float2 y[4];
+                float f[4];
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        if (j + (v >> 1) * kStep >= Q) break;
-                        const float2 c = mis_term(I.law, x, ys4[v], fs4[v], w1, w2, I.cum9[s], alpha, R, I);
-                        sx.add(c.x);
-                        sy.add(c.y);
-                    }
-                    ya = yc;
-                    yb = yd;
-                    fa = fc;
-                    fb = fd;
+                for (int v = 0; v < 4; ++v) {
+                    const int j = j0 + kAccLanes * v;
+                    y[v] = live && j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
+                    f[v] = live && j < Q ? a.fv[base + j] : 0.f;
                 }
-            } else {
-                for (int j0 = sub; j0 < Q; j0 += 4 * kAccLanes) {
-                    float2 y[4];
-                    float f[4];
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        const int j = j0 + kAccLanes * v;
-                        y[v] = live && j < Q ? a.ys[base + j] : make_float2(0.f, 0.f);
-                        f[v] = live && j < Q ? a.fv[base + j] : 0.f;
-                    }
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        if (j0 + kAccLanes * v >= Q) break;
-                        const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
-                        sx.add(c.x);
-                        sy.add(c.y);
-                    }
+                for (int v = 0; v < 4; ++v) {
+                    if (j0 + kAccLanes * v >= Q) break;
+                    const float2 c = mis_term(I.law, x, y[v], f[v], w1, w2, I.cum9[s], alpha, R, I);
+                    sx.add(c.x);
+                    sy.add(c.y);
                 }
             }
             group_sum_comp_pair<kAccLanes>(sx.s, sx.c);
