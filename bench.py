@@ -153,8 +153,8 @@ def reports(rank: int) -> bool:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
 #       -k regex:k_eval -s 1 -c 1 python bench.py --workload tg512s --k 7 --qpt 4 ...
 EVAL_DRAM_BYTES_PER_LAUNCH = {
-    "tg2048": {"bytes": 16 * 4.220e9, "source": "ncu capture of tg512s (4.220 GB per launch) x 16"},
-    "tg512s": {"bytes": 4.220e9, "source": "ncu capture of tg512s"},
+    "tg2048": {"bytes": 16 * 4.248e9, "source": "ncu capture of tg512s (4.248 GB per launch) x 16"},
+    "tg512s": {"bytes": 4.248e9, "source": "ncu capture of tg512s"},
 }
 
 
