@@ -50,9 +50,13 @@ inline void FillCells_cuda(int rshx, int rshy, float Lx, float Ly, int N, const 
                 "FillCells_cuda");
 }
 
-// CountingSort_cuda (src/cuda/hash.cu:71-91): the cell count is inferred from
-// vp_cell (one device-to-host read), as the reference's signature has none.
-inline void CountingSort_cuda(int N, int* cell_num, const int* cell_acc, const int* vp_cell, int* vp_map) {
-    vpmc::check(vpmc_counting_sort(vpmc::default_context(), N, 0, cell_num, cell_acc, vp_cell, vp_map),
+// CountingSort_cuda (src/cuda/hash.cu:71-91).  The reference's five-argument
+// call has no cell count: it is then inferred from vp_cell (one device-to-host
+// read; the reference synchronises the device at this point too).  A caller
+// that knows it (rshx * rshy) passes it as `ncell` and the call stays on the
+// device until its final wait.
+inline void CountingSort_cuda(int N, int* cell_num, const int* cell_acc, const int* vp_cell, int* vp_map,
+                              int ncell = 0) {
+    vpmc::check(vpmc_counting_sort(vpmc::default_context(), N, ncell, cell_num, cell_acc, vp_cell, vp_map),
                 "CountingSort_cuda");
 }

@@ -24,6 +24,8 @@ the `-m gpu` tests pin against the CPU oracle.  Synthetic inputs only.
                       velocity RMS error against the FP64 direct sum at 4096
                       particles (seed 2) for N1 = N2 in {16, 32, 64, 128, 256},
                       plus the FP64 path's error at N1 = N2 = 64.
+  --study variance    the same workload at N1 = N2 = 64: per-particle variance
+                      of the unbiased and the reference estimator laws.
 """
 from __future__ import annotations
 
@@ -329,16 +331,57 @@ def study_error_cost(args):
                               "mollified direct sum; it falls as 1/sqrt(samples per target)"}))
 
 
+# ------------------------------------------------------------------ variance
+def study_variance(args):
+    """Per-particle variance of the two estimator laws at the bench
+    configuration: S velocity passes (S Philox steps) per law, 4096 particles
+    (generator seed 2).  The reference law's variance is the figure the
+    reference's estimator has (its mean is biased); the unbiased law's is the
+    price of its correct mean."""
+    import torch
+    from vortexparticlemc_cuda_gb300 import phash as P
+    dev = torch.device("cuda", 0)
+    Nx, hwr, n, dt = 2048, 16.0, 64, 2.5e-4
+    S = args.seeds
+    sim, pos, info = make_sim(P, dev, Nx, hwr, n, n, dt, P.LAW_UNBIASED, seed=0)
+    sim.set_tuning(7, 4)
+    p, om, _ = sim.particles()
+    h_w = P.SimParam(Nx=Nx, hwr=hwr).h_w
+    idx = np.random.default_rng(2).choice(len(pos), 4096, replace=False)
+    tsel = torch.from_numpy(idx).to(dev)
+    truth = P.direct_velocity(p, om, P.DIRECT_MOLLIFIED, pts=p[tsel], param=h_w).cpu().numpy()
+    out = {}
+    for name, law in (("unbiased", P.LAW_UNBIASED), ("reference", P.LAW_REFERENCE)):
+        sim.set_law(law)
+        v = np.stack([sim.velocity(step=5000 + k)[tsel].cpu().numpy() for k in range(S)]).astype(np.float64)
+        mean = v.mean(0)
+        out[name] = {"per_component_variance": float(v.var(0, ddof=1).mean()),
+                     "median_per_particle_variance": float(np.median(v.var(0, ddof=1))),
+                     "mean_rel_rms_vs_fp64_direct": rel_rms(mean, truth),
+                     "single_estimate_rel_rms_vs_fp64_direct": float(np.mean([rel_rms(v[k], truth) for k in range(S)]))}
+        log(f"{name}: {out[name]}")
+    out["variance_ratio_unbiased_over_reference"] = (out["unbiased"]["per_component_variance"] /
+                                                     out["reference"]["per_component_variance"])
+    out["median_variance_ratio"] = (out["unbiased"]["median_per_particle_variance"] /
+                                    out["reference"]["median_per_particle_variance"])
+    print(json.dumps({"study": "variance", "workload": dict(Nx=Nx, N=len(pos), hwr=hwr, N1=n, N2=n, seeds=S,
+                                                             queries=4096, query_seed=2), **out,
+                      "note": f"mean of {S} estimates per particle; the reference law's mean is biased "
+                              "(its weights do not match its sampling densities)"}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--study", choices=["precision", "inverse", "error-cost"], required=True)
+    ap.add_argument("--study", choices=["precision", "inverse", "error-cost", "variance"], required=True)
+    ap.add_argument("--seeds", type=int, default=16, help="variance: estimates per particle and law")
     ap.add_argument("--steps", type=int, default=0, help="steps (0: the study's own count)")
     ap.add_argument("--fd-dirs", type=int, default=4, help="inverse: random strength directions")
     ap.add_argument("--fd-pos-dirs", type=int, default=2, help="inverse: random position directions")
     ap.add_argument("--samples", type=int, nargs="+", default=[16, 32, 64, 128, 256])
     ap.add_argument("--fp64", action="store_true", help="error-cost: also the FP64 path at N1 = N2 = 64")
     args = ap.parse_args()
-    {"precision": study_precision, "inverse": study_inverse, "error-cost": study_error_cost}[args.study](args)
+    {"precision": study_precision, "inverse": study_inverse, "error-cost": study_error_cost,
+     "variance": study_variance}[args.study](args)
     return 0
 
 

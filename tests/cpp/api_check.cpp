@@ -85,6 +85,11 @@ int main(int argc, char** argv) {
         dump("all_cell_acc", H.cell_acc.to_host());
         dump("all_vp_sort", H.vp_sort.to_host());
         dump("all_cell_num_after", H.cell_num.to_host());
+        // the same with the cell count given (no device-to-host read)
+        FillCells_cuda(8, 8, 1.f, 1.f, N, raw_ptr(sub), sim.particles_.d_p(), raw_ptr(H.cell_num),
+                       raw_ptr(H.cell_acc), raw_ptr(H.vp_cell));
+        CountingSort_cuda(N, raw_ptr(H.cell_num), raw_ptr(H.cell_acc), raw_ptr(H.vp_cell), raw_ptr(H.vp_sort), 64);
+        dump("all_vp_sort_ncell", H.vp_sort.to_host());
 
         SpatialHasher hasher(16, 16, Backend::CUDA);
         hasher.resize(N);

@@ -53,6 +53,7 @@ def test_free_functions_and_hasher(run):
     assert np.array_equal(run("all_cell_acc", np.int32), ref8["cell_acc"])
     assert np.array_equal(run("all_vp_sort", np.int32), ref8["vp_sort"])
     assert not run("all_cell_num_after", np.int32).any()
+    assert np.array_equal(run("all_vp_sort_ncell", np.int32), run("all_vp_sort", np.int32))
     ref16 = O.hash_build(16, 16, 1.0, 1.0, np.arange(n, dtype=np.int32), pos)
     assert np.array_equal(run("hasher_vp_sort", np.int32), ref16["vp_sort"])
     assert np.array_equal(run("hasher_cell_acc", np.int32), ref16["cell_acc"])

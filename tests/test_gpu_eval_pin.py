@@ -129,3 +129,28 @@ def test_unbiased_mean_within_3se_at_benchmark_tuning(tg512, cuda):
     frac = np.mean(np.abs(z) <= 3.0)
     assert frac >= 0.985, frac
     assert 0.8 < np.mean(z ** 2) < 1.3, np.mean(z ** 2)
+
+
+def test_reference_law_variance_at_benchmark_geometry(tg512, cuda):
+    """The reference law's per-particle variance and mean against the oracle's
+    restatement of the reference GPU kernel's sampling law
+    (monte_carlo_bs_kernel_safe, src/cuda/monte_carlo_bs.cu:144-271) at the
+    benchmark's h_w in cells and samples per target (N1 = N2 = 64), 64 seeds,
+    256 targets: variance within 10%, means within 3 combined standard errors."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    sim, sp, pos, om = tg512
+    sim.set_law(P.LAW_REFERENCE)
+    sim.set_tuning(7, 4)
+    targets = np.random.default_rng(6).choice(len(pos), 256, replace=False)
+    tsel = torch.from_numpy(targets).to(cuda)
+    seeds = 64
+    g = np.stack([sim.velocity(step=300 + s)[tsel].cpu().numpy() for s in range(seeds)]).astype(np.float64)
+    prm = O.SimParam(dt=5e-4, Nx=NX, hwr=HWR, N1=N1, N2=N2)
+    st = O.OracleState(pos, om, prm)
+    cpu = np.stack([O.mc_velocity_omp(st, pos[targets], N1, N2, 1000 * s + 9, law=1)[0]
+                    for s in range(seeds)]).astype(np.float64)
+    var_ratio = g.var(0, ddof=1).mean() / cpu.var(0, ddof=1).mean()
+    assert abs(var_ratio - 1.0) < 0.10, var_ratio
+    z = (g.mean(0) - cpu.mean(0)) / np.sqrt(g.var(0, ddof=1) / seeds + cpu.var(0, ddof=1) / seeds)
+    assert np.mean(np.abs(z) <= 3.0) >= 0.98, np.mean(np.abs(z) <= 3.0)
+    sim.set_law(P.LAW_UNBIASED)
