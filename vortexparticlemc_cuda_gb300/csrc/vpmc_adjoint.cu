@@ -1,7 +1,8 @@
 // vpmc_adjoint.cu -- the adjoint of the plain MIS step (no counterpart in
 // the reference): checkpointed forward record, segment recompute, and per
-// step the FP64 value/gradient field sums at the samples, the per-sample
-// derivatives of the MIS term, and the transposed field sum at the particles.
+// step the value/gradient field sums at the samples (pairs in the forward's
+// precision), the per-sample FP64 derivatives of the MIS term, and the
+// transposed field sum at the particles.
 #include <algorithm>
 #include <vector>
 
@@ -289,7 +290,9 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.fg, 0, 3 * sizeof(double) * size_t(ns), st));
         EvalLaunch L;
-        L.mode = unb ? EVAL_GRAD9_64 : EVAL_GRAD64;
+        // the FP32 path's adjoint sums its pairs in FP32 (into FP64 run sums), the FP64 path's in FP64
+        const bool f32 = s->precision == 32;
+        L.mode = unb ? (f32 ? EVAL_GRAD9_32 : EVAL_GRAD9_64) : (f32 ? EVAL_GRAD32 : EVAL_GRAD64);
         L.qpt = 4;
         L.out_f64 = A.fg;
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
@@ -305,7 +308,7 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         VPMC_TRY(make_items(ctx, s->g, s->g.cstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.dual_out, 0, 3 * sizeof(double) * size_t(s->N), st));
         EvalLaunch D;
-        D.mode = unb ? EVAL_DUAL9_64 : EVAL_DUAL64;
+        D.mode = unb ? (f32 ? EVAL_DUAL9_32 : EVAL_DUAL9_64) : (f32 ? EVAL_DUAL32 : EVAL_DUAL64);
         D.rows = 1;   // the samples are grouped by whole bins
         D.qpt = 4;
         D.out_f64 = A.dual_out;

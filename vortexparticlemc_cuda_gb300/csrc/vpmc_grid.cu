@@ -739,7 +739,10 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     constexpr bool kComp = MODE == EVAL_SPMV32;
     constexpr bool kField64 = MODE == EVAL_FIELD64 || MODE == EVAL_FIELD9_64;
     constexpr bool kGrad = eval_grad(MODE);
-    constexpr bool kDual9 = MODE == EVAL_DUAL9_64;
+    constexpr bool kGrad32 = MODE == EVAL_GRAD32 || MODE == EVAL_GRAD9_32 || MODE == EVAL_DUAL32 || MODE == EVAL_DUAL9_32;
+    constexpr bool kGrad9 = MODE == EVAL_GRAD9_64 || MODE == EVAL_GRAD9_32;
+    constexpr bool kDual9 = MODE == EVAL_DUAL9_64 || MODE == EVAL_DUAL9_32;
+    using GT = typename std::conditional<kGrad32, float, double>::type;
     constexpr bool kDef = eval_deformed(MODE);
     constexpr bool kDefExc = MODE == EVAL_FIELD_F_EXC;
     constexpr bool kPacked = MODE == EVAL_FIELD || MODE == EVAL_FIELD9 || MODE == EVAL_FIELD_F || MODE == EVAL_FIELD9_F;
@@ -1172,19 +1175,20 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         }
                     }
                 } else if constexpr (kGrad) {
-                    // FP64 value and gradient in q of sum w W(|q - c|):
+                    // value and gradient in q of sum w W(|q - c|), pair by pair in GT
+                    // (FP64, or FP32 for the FP32 path's adjoint; run sums into FP64):
                     // dW/dr / r = 2 sigma (3 A r + 2 B) for r < h/2, -6 sigma t^2/(h r) below h
-                    const double hw = double(G.hw), ih = 1.0 / hw;
-                    const double A = 3.0 * ih * ih * ih, B = -3.0 * ih * ih;
-                    double px[QPT], py[QPT], pv[QPT], pgx[QPT], pgy[QPT];
+                    const GT hw = GT(G.hw), ih = GT(1) / hw;
+                    const GT A = GT(3) * ih * ih * ih, B = GT(-3) * ih * ih;
+                    GT px[QPT], py[QPT], pv[QPT], pgx[QPT], pgy[QPT];
                     bool use[QPT];
 #pragma unroll
                     for (int j = 0; j < QPT; ++j) {
-                        px[j] = double(qx[j]) + double(pc.qdx);
-                        py[j] = double(qy[j]) + double(pc.qdy);
-                        pv[j] = pgx[j] = pgy[j] = 0.0;
+                        px[j] = GT(qx[j]) + GT(pc.qdx);
+                        py[j] = GT(qy[j]) + GT(pc.qdy);
+                        pv[j] = pgx[j] = pgy[j] = GT(0);
                         use[j] = true;
-                        if (MODE == EVAL_GRAD9_64) {
+                        if (kGrad9) {
                             const int mx = int(uint32_t(qfl >> (6 * j)) & 7u) - 2 + pc.mx;
                             const int my = int(uint32_t(qfl >> (6 * j + 3)) & 7u) - 2 + pc.my;
                             use[j] = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
@@ -1192,7 +1196,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                     }
                     for (int c = 0; c < cnt; ++c) {
                         const Cand cv = cs[c];
-                        const double cxd = cv.x, cyd = cv.y, wd = double(cv.w) + double(cv.wl);
+                        const GT cxd = cv.x, cyd = cv.y;
+                        const GT wd = kGrad32 ? GT(cv.w) : GT(double(cv.w) + double(cv.wl));
                         bool cuse = true;
                         if (kDual9) {
                             // sample y with unwrapped tile k_y seen through image sxi of
@@ -1204,18 +1209,18 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         if (!cuse) continue;
 #pragma unroll
                         for (int j = 0; j < QPT; ++j) {
-                            const double dx = px[j] - cxd, dy = py[j] - cyd;   // q - c
-                            const double r2 = dx * dx + dy * dy;
-                            const double r = sqrt(r2);
+                            const GT dx = px[j] - cxd, dy = py[j] - cyd;   // q - c
+                            const GT r2 = dx * dx + dy * dy;
+                            const GT r = sqrt(r2);
                             if (r >= hw) continue;
-                            const double t = 1.0 - ih * r;
-                            double v, dr;   // W / 2 sigma and its r-derivative over r
-                            if (r <= 0.5 * hw) {
-                                v = 0.5 + r2 * (A * r + B);
-                                dr = 3.0 * A * r + 2.0 * B;
+                            const GT t = GT(1) - ih * r;
+                            GT v, dr;   // W / 2 sigma and its r-derivative over r
+                            if (r <= GT(0.5) * hw) {
+                                v = GT(0.5) + r2 * (A * r + B);
+                                dr = GT(3) * A * r + GT(2) * B;
                             } else {
                                 v = t * t * t;
-                                dr = -3.0 * t * t * ih / r;
+                                dr = GT(-3) * t * t * ih / r;
                             }
                             pv[j] += wd * v;
                             pgx[j] += wd * dr * dx;
@@ -1225,9 +1230,9 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
 #pragma unroll
                     for (int j = 0; j < QPT; ++j) {
                         if (!use[j]) continue;
-                        acc[j] += pv[j];
-                        accg[j][0] += pgx[j];
-                        accg[j][1] += pgy[j];
+                        acc[j] += double(pv[j]);
+                        accg[j][0] += double(pgx[j]);
+                        accg[j][1] += double(pgy[j]);
                         part[j] = 0.0;
                     }
                 } else if constexpr (kField64) {
@@ -1616,6 +1621,10 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
         case EVAL_GRAD9_64: return launch_eval_t<EVAL_GRAD9_64, 4>(ctx, a);
         case EVAL_DUAL64: return launch_eval_t<EVAL_DUAL64, 4>(ctx, a);
         case EVAL_DUAL9_64: return launch_eval_t<EVAL_DUAL9_64, 4>(ctx, a);
+        case EVAL_GRAD32: return launch_eval_t<EVAL_GRAD32, 4>(ctx, a);
+        case EVAL_GRAD9_32: return launch_eval_t<EVAL_GRAD9_32, 4>(ctx, a);
+        case EVAL_DUAL32: return launch_eval_t<EVAL_DUAL32, 4>(ctx, a);
+        case EVAL_DUAL9_32: return launch_eval_t<EVAL_DUAL9_32, 4>(ctx, a);
         case EVAL_FIELD64: return launch_eval_t<EVAL_FIELD64, 4>(ctx, a);
         case EVAL_FIELD9_64: return launch_eval_t<EVAL_FIELD9_64, 4>(ctx, a);
         default: return VPMC_ERR_INVALID;

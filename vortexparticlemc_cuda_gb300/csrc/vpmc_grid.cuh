@@ -84,10 +84,17 @@ enum EvalMode : int {
     EVAL_GRAD9_64 = 11,  // same with the FIELD9 image mask of the query
     EVAL_DUAL64 = 12,    // queries are particles, candidates are samples: G(q) = sum a_s W(|q - y_s|)
     EVAL_DUAL9_64 = 13,  // same with each sample's FIELD9 image mask (flags in the candidate's pad word)
+    // the same four with the pairs in FP32 (weights w only) and the run sums in FP64:
+    // the adjoint of the FP32-compensated step
+    EVAL_GRAD32 = 14,
+    EVAL_GRAD9_32 = 15,
+    EVAL_DUAL32 = 16,
+    EVAL_DUAL9_32 = 17,
 };
 
 __host__ __device__ constexpr bool eval_grad(int mode) {
-    return mode == EVAL_GRAD64 || mode == EVAL_GRAD9_64 || mode == EVAL_DUAL64 || mode == EVAL_DUAL9_64;
+    return mode == EVAL_GRAD64 || mode == EVAL_GRAD9_64 || mode == EVAL_DUAL64 || mode == EVAL_DUAL9_64 ||
+           mode == EVAL_GRAD32 || mode == EVAL_GRAD9_32 || mode == EVAL_DUAL32 || mode == EVAL_DUAL9_32;
 }
 
 __host__ __device__ constexpr bool eval_deformed(int mode) {
