@@ -389,10 +389,10 @@ int vpmc_sim_vorticity_grid(vpmc_sim* sim, int inst, int res_x, int res_y, int s
  *     segment from its checkpoint and run the adjoint steps backwards; writes
  *     dL/dX_0 (2N doubles) and dL/domega (N doubles); the simulation is left
  *     in the recorded final state.  The trajectory is the forward's (its
- *     precision); the adjoint's field values and gradients at the samples and
- *     its transposed sums take their pairs in the forward's precision (FP32
- *     pairs summed into FP64 per run for the FP32 path), and every MIS-term
- *     derivative and accumulation is FP64.
+ *     precision); the adjoint's field values and gradients at the samples
+ *     take their pairs in the forward's precision (FP32 pairs summed into
+ *     FP64 per run for the FP32 path); its transposed sums, every MIS-term
+ *     derivative and every accumulation are FP64.
  *     flags: VPMC_ADJ_SCORE adds the score-function term of the discrete
  *     branch-1 draw (P(I = J) = |omega_J| / Omega), which makes dL/domega an
  *     unbiased estimate of the gradient of the expected trajectory; without

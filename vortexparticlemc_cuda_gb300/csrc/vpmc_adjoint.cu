@@ -290,7 +290,9 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.fg, 0, 3 * sizeof(double) * size_t(ns), st));
         EvalLaunch L;
-        // the FP32 path's adjoint sums its pairs in FP32 (into FP64 run sums), the FP64 path's in FP64
+        // field values and gradients at the samples: the FP32 path's adjoint sums
+        // its pairs in FP32 (into FP64 run sums; the candidates are the particles
+        // in grid order, so the sums are fixed-order), the FP64 path's in FP64
         const bool f32 = s->precision == 32;
         L.mode = unb ? (f32 ? EVAL_GRAD9_32 : EVAL_GRAD9_64) : (f32 ? EVAL_GRAD32 : EVAL_GRAD64);
         L.qpt = 4;
@@ -308,7 +310,10 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         VPMC_TRY(make_items(ctx, s->g, s->g.cstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.dual_out, 0, 3 * sizeof(double) * size_t(s->N), st));
         EvalLaunch D;
-        D.mode = unb ? (f32 ? EVAL_DUAL9_32 : EVAL_DUAL9_64) : (f32 ? EVAL_DUAL32 : EVAL_DUAL64);
+        // the transposed sums stay FP64 on both paths: their weights dc/df take
+        // both signs and the samples reach the sums in placement order, which is
+        // not fixed, so FP32 pairs would make the gradient depend on that order
+        D.mode = unb ? EVAL_DUAL9_64 : EVAL_DUAL64;
         D.rows = 1;   // the samples are grouped by whole bins
         D.qpt = 4;
         D.out_f64 = A.dual_out;
