@@ -159,44 +159,21 @@ __global__ void __launch_bounds__(256) k_adj_terms(AdjArgs a) {
     }
 }
 
-// Samples (already grouped by bin in query-record order) as candidates of the
-// transposed sum: weight 2 sigma dc/df (FP32 hi + lo), image flags in pad.
-__global__ void k_adj_dual_cand(const QRec* __restrict__ qrec, const uint32_t* __restrict__ total, long M,
-                                const double* __restrict__ as, const uint32_t* __restrict__ qbin,
-                                const GridInst* __restrict__ inst, int n_inst, Cand* __restrict__ out) {
-    const long n = min(long(*total), M);
-    for (long k = long(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += long(gridDim.x) * blockDim.x) {
-        const QRec r = qrec[k];
-        const uint32_t b = qbin[r.id];
-        int lo = 0, hi = n_inst - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (uint32_t(inst[mid].bin_base) <= b) lo = mid; else hi = mid - 1;
-        }
-        const double h = inst[lo].hw;
-        const double w = as[r.id] * (80.0 / (7.0 * kPiD * h * h));
-        const float wh = float(w);
-        out[k] = Cand{r.x, r.x, r.y, r.y, wh, wh, float(w - double(wh)), __uint_as_float(r.flags)};
-    }
-}
-
-// Particles in bin order as queries (self queries of the grid).
-__global__ void k_adj_self(const Cand* __restrict__ cand, const uint32_t* __restrict__ perm,
-                           const uint32_t* __restrict__ start, long n, uint32_t nbins, QRec* __restrict__ q) {
-    const long nv = start[nbins];
-    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv && p < n; p += long(gridDim.x) * blockDim.x)
-        q[p] = QRec{cand[p].x, cand[p].y, perm[p], (2u) | (2u << 3)};
-}
-
-__global__ void k_adj_sources(const float* __restrict__ omega, long n, const double* __restrict__ dual,
-                              double* __restrict__ lam, double* __restrict__ gom) {
-    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+// The transposed sums (by grid slot) onto the particles: dL/domega through the
+// strength, lambda through the position (the weight |omega| of each particle's
+// kernel).  Each particle holds at most one slot (sign-split sets).
+__global__ void k_adj_sources(const float* __restrict__ omega, const uint32_t* __restrict__ perm,
+                              const uint32_t* __restrict__ cstart, uint32_t nbins, long n,
+                              const double* __restrict__ dual, double* __restrict__ lam, double* __restrict__ gom) {
+    const long nv = min(long(cstart[nbins]), n);
+    for (long p = long(blockIdx.x) * blockDim.x + threadIdx.x; p < nv; p += long(gridDim.x) * blockDim.x) {
+        const uint32_t i = perm[p];
         const float w = omega[i];
         if (w == 0.f) continue;
         const double aw = fabs(double(w));
-        gom[i] += (w > 0.f ? 1.0 : -1.0) * dual[3 * i];
-        lam[2 * i] += aw * dual[3 * i + 1];
-        lam[2 * i + 1] += aw * dual[3 * i + 2];
+        gom[i] += (w > 0.f ? 1.0 : -1.0) * dual[3 * p];
+        lam[2 * i] += aw * dual[3 * p + 1];
+        lam[2 * i + 1] += aw * dual[3 * p + 2];
     }
 }
 
@@ -221,15 +198,12 @@ __global__ void k_adj_cum(const InstMC* __restrict__ mc, int n_inst, const float
 }
 
 // Adjoint working set (allocated on first use): per chunk of samples the
-// source index, FP64 value + gradient, dc/df and the transposed candidates;
-// per particle the self queries, the transposed sums, two lambda buffers and
-// dL/domega.
+// source index, FP64 value + gradient and dc/df; per particle the transposed
+// sums (by grid slot), two lambda buffers and dL/domega.
 struct AdjBufs {
     int* src;
     double* fg;
     double* as;
-    Cand* dual;
-    QRec* selfq;
     double* dual_out;
     double* lam[2];
     double* gom;
@@ -244,8 +218,6 @@ int adj_bufs(vpmc_sim* s, AdjBufs* A) {
         A->src = c.take<int>(size_t(ns));
         A->fg = c.take<double>(3 * size_t(ns));
         A->as = c.take<double>(size_t(ns));
-        A->dual = c.take<Cand>(size_t(ns));
-        A->selfq = c.take<QRec>(size_t(s->N));
         A->dual_out = c.take<double>(3 * size_t(s->N));
         A->lam[0] = c.take<double>(2 * size_t(s->N));
         A->lam[1] = c.take<double>(2 * size_t(s->N));
@@ -268,8 +240,6 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
     vpmc_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     VPMC_TRY(grid_build(ctx, s->g, s->pos, s->omega, SET_SIGN_SPLIT));
-    VPMC_LAUNCH(k_adj_self, blocks_for(s->N), 256, 0, st, s->g.cand, s->g.perm, s->g.cstart, s->N,
-                uint32_t(s->g.nbins), A.selfq);
     VPMC_CUDA(cudaMemcpyAsync(lam_out, lam_in, 2 * sizeof(double) * size_t(s->N), cudaMemcpyDeviceToDevice, st));
     VPMC_CUDA(cudaMemsetAsync(A.dcum, 0, 2 * sizeof(double) * size_t(s->n_inst), st));
     if (score) {
@@ -301,24 +271,19 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         AdjArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, A.fg, A.src, s->cum64, t0, nt, s->N1, s->N2, lam_in, lam_out,
                    A.as, A.dcum, score ? A.gsc : nullptr, A.csum};
         VPMC_LAUNCH(k_adj_terms, blocks_for(nt * 32), 256, 0, st, aa);
-        // transposed sum: particles query the chunk's samples
-        VPMC_LAUNCH(k_adj_dual_cand, blocks_for(ns), 256, 0, st, s->q.qrec, s->q.qstart + s->g.nbins, ns, A.as,
-                    s->q.qbin, s->g.inst, s->g.n_inst, A.dual);
-        GridBufs gd = s->g;
-        gd.start = s->q.qstart;
-        gd.cand = A.dual;
-        VPMC_TRY(make_items(ctx, s->g, s->g.cstart, s->it, query_chunk(4)));
+        // transposed sums from the sample side: the same items, each sample
+        // weighted by its dc/df, every in-support (sample, particle) pair adding
+        // a_s W and a_s dW/dx_p to the particle's slot
+        VPMC_TRY(make_items(ctx, s->g, s->q.qstart, s->it, query_chunk(4)));
         VPMC_CUDA(cudaMemsetAsync(A.dual_out, 0, 3 * sizeof(double) * size_t(s->N), st));
         EvalLaunch D;
-        // the transposed sums stay FP64 on both paths: their weights dc/df take
-        // both signs and the samples reach the sums in placement order, which is
-        // not fixed, so FP32 pairs would make the gradient depend on that order
-        D.mode = unb ? EVAL_DUAL9_64 : EVAL_DUAL64;
-        D.rows = 1;   // the samples are grouped by whole bins
+        D.mode = unb ? (f32 ? EVAL_SCAT9_32 : EVAL_SCAT9_64) : (f32 ? EVAL_SCAT32 : EVAL_SCAT64);
         D.qpt = 4;
         D.out_f64 = A.dual_out;
-        VPMC_TRY(launch_eval(ctx, gd, A.selfq, s->it, D));
-        VPMC_LAUNCH(k_adj_sources, blocks_for(s->N), 256, 0, st, s->omega, s->N, A.dual_out, lam_out, A.gom);
+        D.qweight = A.as;
+        VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, D));
+        VPMC_LAUNCH(k_adj_sources, blocks_for(s->N), 256, 0, st, s->omega, s->g.perm, s->g.cstart,
+                    uint32_t(s->g.nbins), s->N, A.dual_out, lam_out, A.gom);
     }
     VPMC_LAUNCH(k_adj_cum, blocks_for(s->N), 256, 0, st, s->d_mc, s->n_inst, s->omega, s->N, A.dcum, s->cum64,
                 score ? A.gsc : nullptr, A.csum, A.gom);

@@ -604,6 +604,7 @@ struct EvalArgs {
     double* out_f64;
     unsigned* flags;
     uint32_t wait_limit;      // polls of a staging wait before the kernel gives up
+    const double* qweight;    // SCAT modes: the weight of each query (by id)
 };
 
 // Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction
@@ -714,6 +715,88 @@ __device__ __forceinline__ void packed_run_f(const CandF* __restrict__ cs, int c
     }
 }
 
+// s + e += x with s the running sum and e the running sum of its rounding errors
+// (Knuth's TwoSum; the products are formed with __fmul_rn so no FMA contraction
+// can fold them into the sum and break the exact error term).
+__device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp)));
+    s = t;
+}
+
+// The transposed sums of one staged batch, from the sample side (SCAT modes).
+// The item's samples sit in s_sq (x, y, weight hi, weight lo; image flags in
+// s_sqf); the batch's particles are staged back to back in s_cand.  Lane l takes
+// staged particles l, l + 32, ... (whatever run each lies in), sums over all
+// the item's samples the terms a_s W(|x_p - y_s|) and a_s dW/dx_p in the
+// pair's image, and adds them to out[3 slot + {0, 1, 2}] with one FP64 atomic
+// each, slot = the particle's candidate index.  The pair is the one the GRAD
+// modes form with the roles of query and candidate swapped: the sample seen
+// through the run's image is y + qdx, so x_p - y_s = (c - qdx) - q.
+template <typename ST, bool K9>
+__device__ __forceinline__ void scat_batch(const Cand* __restrict__ s_cand, const BatchPiece* s_bp,
+                                           const Piece* s_pc, int nbp, uint32_t btot, const float4* s_sq,
+                                           const uint8_t* s_sqf, int nq, const GridInst& G,
+                                           double* __restrict__ out) {
+    constexpr bool k32 = std::is_same<ST, float>::value;
+    const int lane = threadIdx.x & 31;
+    const ST hw = ST(G.hw), ih = ST(1) / hw;
+    const ST A = ST(3) * ih * ih * ih, B = ST(-3) * ih * ih;
+    int b = 0;
+    for (uint32_t i = uint32_t(lane); i < btot; i += 32u) {
+        while (b + 1 < nbp && s_bp[b + 1].soff <= i) ++b;
+        const BatchPiece bp = s_bp[b];
+        const Piece pc = s_pc[bp.piece];
+        const Cand cv = s_cand[i];
+        const ST cx = ST(cv.x) - ST(pc.qdx), cy = ST(cv.y) - ST(pc.qdy);
+        ST sv = ST(0), sgx = ST(0), sgy = ST(0);
+        float ev = 0.f, egx = 0.f, egy = 0.f;   // FP32 pairs: the sums' error terms
+        for (int j = 0; j < nq; ++j) {
+            if (K9) {
+                // sample in unwrapped tile k_y paired through image sxi of this
+                // run: the source image it sees is k_y + sxi
+                const uint32_t fl = s_sqf[j];
+                const int mx = int(fl & 7u) - 2 + pc.mx, my = int((fl >> 3) & 7u) - 2 + pc.my;
+                if (mx < -1 || mx > 1 || my < -1 || my > 1) continue;
+            }
+            const float4 q = s_sq[j];
+            const ST dx = cx - ST(q.x), dy = cy - ST(q.y);   // x_p - y_s
+            const ST r2 = dx * dx + dy * dy;
+            const ST r = sqrt(r2);
+            if (r >= hw) continue;
+            const ST t = ST(1) - ih * r;
+            ST v, dr;   // W / 2 sigma and its r-derivative over r
+            if (r <= ST(0.5) * hw) {
+                v = ST(0.5) + r2 * (A * r + B);
+                dr = ST(3) * A * r + ST(2) * B;
+            } else {
+                v = t * t * t;
+                dr = ST(-3) * t * t * ih / r;
+            }
+            if constexpr (k32) {
+                const float w = q.z;
+                const float wdr = __fmul_rn(w, dr);
+                two_sum_acc(sv, ev, __fmul_rn(w, v));
+                two_sum_acc(sgx, egx, __fmul_rn(wdr, dx));
+                two_sum_acc(sgy, egy, __fmul_rn(wdr, dy));
+            } else {
+                const double w = double(q.z) + double(q.w);
+                sv += w * v;
+                sgx += w * dr * dx;
+                sgy += w * dr * dy;
+            }
+        }
+        const double gv = double(sv) + double(ev), ggx = double(sgx) + double(egx), ggy = double(sgy) + double(egy);
+        if (gv != 0.0 || ggx != 0.0 || ggy != 0.0) {
+            double* o = out + 3 * (size_t(bp.gstart) + size_t(i - bp.soff));
+            atomicAdd(o, gv);
+            atomicAdd(o + 1, ggx);
+            atomicAdd(o + 2, ggy);
+        }
+    }
+}
+
 // The packed FP32 kernels run one-warp CTAs, 24 per SM (their 6.25 KB staging
 // buffers fit 24 times in shared memory; 85 registers a thread at most) with 4
 // queries per thread, 16 per SM with 6 and 12 with 8.  One warp per CTA: no warp of an item
@@ -734,14 +817,19 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     __shared__ uint32_t s_cur_off, s_btot, s_item;
     __shared__ float s_ox, s_oy;
     __shared__ __align__(8) uint64_t s_bar;
+    constexpr bool kScat = eval_scat(MODE);
+    constexpr int kScatQ = kScat ? kEvalThreads * QPT : 1;   // an item's queries (make_items' chunk)
+    __shared__ float4 s_sq[kScatQ];
+    __shared__ uint8_t s_sqf[kScatQ];
 
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
     constexpr bool kField64 = MODE == EVAL_FIELD64 || MODE == EVAL_FIELD9_64;
     constexpr bool kGrad = eval_grad(MODE);
-    constexpr bool kGrad32 = MODE == EVAL_GRAD32 || MODE == EVAL_GRAD9_32 || MODE == EVAL_DUAL32 || MODE == EVAL_DUAL9_32;
+    constexpr bool kGrad32 = MODE == EVAL_GRAD32 || MODE == EVAL_GRAD9_32;
     constexpr bool kGrad9 = MODE == EVAL_GRAD9_64 || MODE == EVAL_GRAD9_32;
-    constexpr bool kDual9 = MODE == EVAL_DUAL9_64 || MODE == EVAL_DUAL9_32;
+    constexpr bool kScat9 = MODE == EVAL_SCAT9_64 || MODE == EVAL_SCAT9_32;
+    using ST = typename std::conditional<MODE == EVAL_SCAT32 || MODE == EVAL_SCAT9_32, float, double>::type;
     using GT = typename std::conditional<kGrad32, float, double>::type;
     constexpr bool kDef = eval_deformed(MODE);
     constexpr bool kDefExc = MODE == EVAL_FIELD_F_EXC;
@@ -926,6 +1014,18 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             acc_c[j] = 0.f;
             if constexpr (kGrad) accg[j][0] = accg[j][1] = 0.0;
         }
+        if constexpr (kScat) {
+            // the item's samples with their weights a_s 2 sigma (FP32 hi + lo)
+            const double sig2 = 80.0 / (7.0 * kPiD * double(G.hw) * double(G.hw));
+            for (uint32_t k = uint32_t(tid); k < it.qcnt && k < uint32_t(kScatQ); k += kEvalThreads) {
+                const QRec r = a.qrec[it.qbeg + k];
+                const double w = a.qweight[r.id] * sig2;
+                const float wh = float(w);
+                s_sq[k] = make_float4(r.x, r.y, wh, float(w - double(wh)));
+                s_sqf[k] = uint8_t(r.flags & 63u);
+            }
+            if (tid == 0 && it.qcnt > uint32_t(kScatQ)) atomicOr(a.flags, FLAG_CAPACITY);
+        }
         __syncthreads();
         if constexpr (kPacked) {
             // bounding box of this warp's queries in the bin's frame
@@ -1028,6 +1128,9 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             }
 
             const int nbp = s_nbp;
+            if constexpr (kScat)
+                scat_batch<ST, kScat9>(s_cand, s_bp, s_pc, nbp, s_btot, s_sq, s_sqf,
+                                       min(int(it.qcnt), kScatQ), G, a.out_f64);
             if constexpr (kPacked) {
                 // staged candidates -> image-shifted, bin-local coordinates + kappa c2
                 // (kappa = -3/h^2 scales every squared distance, see packed_run)
@@ -1068,7 +1171,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 if (tid == 0) s_pre = 0;
                 if (s_abort) break;   // (a thread whose wait expired rewrote stale bytes: unused)
             }
-            for (int b = 0; b < nbp; ++b) {
+            for (int b = 0; b < (kScat ? 0 : nbp); ++b) {
                 const BatchPiece bp = s_bp[b];
                 const Piece pc = s_pc[bp.piece];
                 int cnt = int(bp.cnt);
@@ -1198,15 +1301,6 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                         const Cand cv = cs[c];
                         const GT cxd = cv.x, cyd = cv.y;
                         const GT wd = kGrad32 ? GT(cv.w) : GT(double(cv.w) + double(cv.wl));
-                        bool cuse = true;
-                        if (kDual9) {
-                            // sample y with unwrapped tile k_y seen through image sxi of
-                            // this run: the source image it pairs with is k_y - sxi
-                            const uint32_t fl = __float_as_uint(cv.pad);
-                            const int mx = int(fl & 7u) - 2 - pc.mx, my = int((fl >> 3) & 7u) - 2 - pc.my;
-                            cuse = mx >= -1 && mx <= 1 && my >= -1 && my <= 1;
-                        }
-                        if (!cuse) continue;
 #pragma unroll
                         for (int j = 0; j < QPT; ++j) {
                             const GT dx = px[j] - cxd, dy = py[j] - cyd;   // q - c
@@ -1337,7 +1431,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
         }
         if (s_abort) break;
 #pragma unroll
-        for (int j = 0; j < QPT; ++j) {
+        for (int j = 0; j < QPT && !kScat; ++j) {
             if (!qv[j]) continue;
             if constexpr (kGrad) {
                 a.out_f64[3 * size_t(qid[j])] = acc[j];
@@ -1586,8 +1680,9 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
     if (eval_deformed(L.mode) && !g.candf) return VPMC_ERR_INVALID;
+    if (eval_scat(L.mode) && (!L.qweight || !L.out_f64 || L.qpt != 4)) return VPMC_ERR_INVALID;
     EvalArgs a{g.inst, g.start, L.rows > 0 ? L.rows : g.rows, g.cand, g.candf, qrec, it.items, it.n_items, it.counter,
-               L.out_f32, L.out_f64, ctx->d_flags, ctx->wait_limit};
+               L.out_f32, L.out_f64, ctx->d_flags, ctx->wait_limit, L.qweight};
     switch (L.mode) {
         case EVAL_FIELD:
             if (L.qpt == 8) return launch_eval_t<EVAL_FIELD, 8>(ctx, a);
@@ -1619,12 +1714,12 @@ int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs
             return launch_eval_t<EVAL_FIELD_F_EXC, 4>(ctx, a);
         case EVAL_GRAD64: return launch_eval_t<EVAL_GRAD64, 4>(ctx, a);
         case EVAL_GRAD9_64: return launch_eval_t<EVAL_GRAD9_64, 4>(ctx, a);
-        case EVAL_DUAL64: return launch_eval_t<EVAL_DUAL64, 4>(ctx, a);
-        case EVAL_DUAL9_64: return launch_eval_t<EVAL_DUAL9_64, 4>(ctx, a);
         case EVAL_GRAD32: return launch_eval_t<EVAL_GRAD32, 4>(ctx, a);
         case EVAL_GRAD9_32: return launch_eval_t<EVAL_GRAD9_32, 4>(ctx, a);
-        case EVAL_DUAL32: return launch_eval_t<EVAL_DUAL32, 4>(ctx, a);
-        case EVAL_DUAL9_32: return launch_eval_t<EVAL_DUAL9_32, 4>(ctx, a);
+        case EVAL_SCAT64: return launch_eval_t<EVAL_SCAT64, 4>(ctx, a);
+        case EVAL_SCAT9_64: return launch_eval_t<EVAL_SCAT9_64, 4>(ctx, a);
+        case EVAL_SCAT32: return launch_eval_t<EVAL_SCAT32, 4>(ctx, a);
+        case EVAL_SCAT9_32: return launch_eval_t<EVAL_SCAT9_32, 4>(ctx, a);
         case EVAL_FIELD64: return launch_eval_t<EVAL_FIELD64, 4>(ctx, a);
         case EVAL_FIELD9_64: return launch_eval_t<EVAL_FIELD9_64, 4>(ctx, a);
         default: return VPMC_ERR_INVALID;

@@ -82,19 +82,30 @@ enum EvalMode : int {
     // FP64 value and gradient (adjoint): out_f64[3 id + {0, 1, 2}] = {f, df/dqx, df/dqy}
     EVAL_GRAD64 = 10,    // f(q) = sum w W(|q - c|)
     EVAL_GRAD9_64 = 11,  // same with the FIELD9 image mask of the query
-    EVAL_DUAL64 = 12,    // queries are particles, candidates are samples: G(q) = sum a_s W(|q - y_s|)
-    EVAL_DUAL9_64 = 13,  // same with each sample's FIELD9 image mask (flags in the candidate's pad word)
-    // the same four with the pairs in FP32 (weights w only) and the run sums in FP64:
-    // the adjoint of the FP32-compensated step
-    EVAL_GRAD32 = 14,
-    EVAL_GRAD9_32 = 15,
-    EVAL_DUAL32 = 16,
-    EVAL_DUAL9_32 = 17,
+    // the two GRAD modes with the pairs in FP32 (weights w only) and the run sums
+    // in FP64: the adjoint of the FP32-compensated step
+    EVAL_GRAD32 = 12,
+    EVAL_GRAD9_32 = 13,
+    // the transposed sums G(x_p) = sum_s a_s W(|x_p - y_s|) and its gradient,
+    // computed from the sample side: the queries are the samples (weight
+    // qweight[id] * 2 sigma), the candidates the particles;
+    // out_f64[3 slot + {0, 1, 2}] += {sum_s a_s W, sum_s a_s dW/dx_p} with slot
+    // the particle's candidate index (grid order), one FP64 atomic per
+    // (item, particle).  SCAT*_64: pairs in FP64; SCAT*_32: pairs in FP32, each
+    // particle's sum over an item's samples compensated (TwoSum), so the result
+    // does not depend on the samples' placement order beyond FP64 rounding.
+    EVAL_SCAT64 = 14,
+    EVAL_SCAT9_64 = 15,  // with each sample's FIELD9 image mask
+    EVAL_SCAT32 = 16,
+    EVAL_SCAT9_32 = 17,
 };
 
 __host__ __device__ constexpr bool eval_grad(int mode) {
-    return mode == EVAL_GRAD64 || mode == EVAL_GRAD9_64 || mode == EVAL_DUAL64 || mode == EVAL_DUAL9_64 ||
-           mode == EVAL_GRAD32 || mode == EVAL_GRAD9_32 || mode == EVAL_DUAL32 || mode == EVAL_DUAL9_32;
+    return mode == EVAL_GRAD64 || mode == EVAL_GRAD9_64 || mode == EVAL_GRAD32 || mode == EVAL_GRAD9_32;
+}
+
+__host__ __device__ constexpr bool eval_scat(int mode) {
+    return mode == EVAL_SCAT64 || mode == EVAL_SCAT9_64 || mode == EVAL_SCAT32 || mode == EVAL_SCAT9_32;
 }
 
 __host__ __device__ constexpr bool eval_deformed(int mode) {
@@ -206,6 +217,7 @@ struct EvalLaunch {
     int qpt = 4;               // queries per thread (FIELD modes: 4 or 8; others: 4)
     float* out_f32 = nullptr;
     double* out_f64 = nullptr;
+    const double* qweight = nullptr;   // SCAT modes: weight of each query, by query id
 };
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L);
 
