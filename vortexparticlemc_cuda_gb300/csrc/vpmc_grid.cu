@@ -725,11 +725,40 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
     s = t;
 }
 
+// W / 2 sigma of the cubic spline and its r-derivative over r, for FP32 pairs
+// without a branch: one reciprocal square root gives r and 1/r, the inner and
+// outer pieces are selected, and beyond the support t = (1 - r/h)+ = 0 makes
+// both exactly zero (r > h/2 there).  r2 is floored at 1e-30, where the inner
+// piece gives v = 1/2 and a zero gradient term (dx = dy = 0).
+__device__ __forceinline__ void spline_vdr_f32(float r2, float hw, float ih, float A, float B, float& v, float& dr) {
+    r2 = fmaxf(r2, 1e-30f);
+    const float rs = rsqrtf(r2);
+    const float r = r2 * rs;
+    const float t = fmaxf(fmaf(-ih, r, 1.f), 0.f);
+    const bool inner = r <= 0.5f * hw;
+    v = inner ? fmaf(r2, fmaf(A, r, B), 0.5f) : t * t * t;
+    dr = inner ? fmaf(3.f * A, r, 2.f * B) : -3.f * ih * (t * t) * rs;
+}
+
+// Images a sample may pair through (unbiased law): bit (sx + 1) * 3 + (sy + 1)
+// is set when a run shifted by image (sx, sy) pairs the sample in unwrapped tile
+// k with source image k + s inside {-1, 0, 1}^2 (flags: bits 0-2 kx + 2, 3-5 ky + 2).
+__device__ __forceinline__ uint32_t image_mask9(uint32_t flags) {
+    const int kx = int(flags & 7u) - 2, ky = int((flags >> 3) & 7u) - 2;
+    uint32_t m = 0u;
+#pragma unroll
+    for (int sx = -1; sx <= 1; ++sx)
+#pragma unroll
+        for (int sy = -1; sy <= 1; ++sy)
+            if (kx + sx >= -1 && kx + sx <= 1 && ky + sy >= -1 && ky + sy <= 1) m |= 1u << ((sx + 1) * 3 + (sy + 1));
+    return m;
+}
+
 // The transposed sums of one staged batch, from the sample side (SCAT modes).
-// The item's samples sit in s_sq (x, y, weight hi, weight lo; image flags in
-// s_sqf); the batch's particles are staged back to back in s_cand.  Lane l takes
-// staged particles l, l + 32, ... (whatever run each lies in), sums over all
-// the item's samples the terms a_s W(|x_p - y_s|) and a_s dW/dx_p in the
+// The item's samples sit in s_sq (x, y, weight hi, weight lo; image masks in
+// s_sqm); the batch's particles are staged back to back in s_cand.  Lane l
+// takes staged particles l, l + 32, ... (whatever run each lies in), sums over
+// all the item's samples the terms a_s W(|x_p - y_s|) and a_s dW/dx_p in the
 // pair's image, and adds them to out[3 slot + {0, 1, 2}] with one FP64 atomic
 // each, slot = the particle's candidate index.  The pair is the one the GRAD
 // modes form with the roles of query and candidate swapped: the sample seen
@@ -737,7 +766,7 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
 template <typename ST, bool K9>
 __device__ __forceinline__ void scat_batch(const Cand* __restrict__ s_cand, const BatchPiece* s_bp,
                                            const Piece* s_pc, int nbp, uint32_t btot, const float4* s_sq,
-                                           const uint8_t* s_sqf, int nq, const GridInst& G,
+                                           const uint16_t* s_sqm, int nq, const GridInst& G,
                                            double* __restrict__ out) {
     constexpr bool k32 = std::is_same<ST, float>::value;
     const int lane = threadIdx.x & 31;
@@ -749,38 +778,42 @@ __device__ __forceinline__ void scat_batch(const Cand* __restrict__ s_cand, cons
         const BatchPiece bp = s_bp[b];
         const Piece pc = s_pc[bp.piece];
         const Cand cv = s_cand[i];
+        const uint32_t pbit = uint32_t((pc.mx + 1) * 3 + (pc.my + 1));
         const ST cx = ST(cv.x) - ST(pc.qdx), cy = ST(cv.y) - ST(pc.qdy);
         ST sv = ST(0), sgx = ST(0), sgy = ST(0);
         float ev = 0.f, egx = 0.f, egy = 0.f;   // FP32 pairs: the sums' error terms
-        for (int j = 0; j < nq; ++j) {
-            if (K9) {
-                // sample in unwrapped tile k_y paired through image sxi of this
-                // run: the source image it sees is k_y + sxi
-                const uint32_t fl = s_sqf[j];
-                const int mx = int(fl & 7u) - 2 + pc.mx, my = int((fl >> 3) & 7u) - 2 + pc.my;
-                if (mx < -1 || mx > 1 || my < -1 || my > 1) continue;
-            }
-            const float4 q = s_sq[j];
-            const ST dx = cx - ST(q.x), dy = cy - ST(q.y);   // x_p - y_s
-            const ST r2 = dx * dx + dy * dy;
-            const ST r = sqrt(r2);
-            if (r >= hw) continue;
-            const ST t = ST(1) - ih * r;
-            ST v, dr;   // W / 2 sigma and its r-derivative over r
-            if (r <= ST(0.5) * hw) {
-                v = ST(0.5) + r2 * (A * r + B);
-                dr = ST(3) * A * r + ST(2) * B;
-            } else {
-                v = t * t * t;
-                dr = ST(-3) * t * t * ih / r;
-            }
-            if constexpr (k32) {
-                const float w = q.z;
+        if constexpr (k32) {
+            // branch-free: a pair outside the support or the sample's images adds
+            // exact zeros, which leave the compensated sums unchanged
+            for (int j = 0; j < nq; ++j) {
+                const float4 q = s_sq[j];
+                float w = q.z;
+                if (K9) w = ((uint32_t(s_sqm[j]) >> pbit) & 1u) ? w : 0.f;
+                const float dx = cx - q.x, dy = cy - q.y;   // x_p - y_s
+                float v, dr;
+                spline_vdr_f32(fmaf(dx, dx, dy * dy), hw, ih, A, B, v, dr);
                 const float wdr = __fmul_rn(w, dr);
                 two_sum_acc(sv, ev, __fmul_rn(w, v));
                 two_sum_acc(sgx, egx, __fmul_rn(wdr, dx));
                 two_sum_acc(sgy, egy, __fmul_rn(wdr, dy));
-            } else {
+            }
+        } else {
+            for (int j = 0; j < nq; ++j) {
+                if (K9 && !((uint32_t(s_sqm[j]) >> pbit) & 1u)) continue;
+                const float4 q = s_sq[j];
+                const double dx = cx - double(q.x), dy = cy - double(q.y);   // x_p - y_s
+                const double r2 = dx * dx + dy * dy;
+                const double r = sqrt(r2);
+                if (r >= hw) continue;
+                const double t = 1.0 - ih * r;
+                double v, dr;   // W / 2 sigma and its r-derivative over r
+                if (r <= 0.5 * hw) {
+                    v = 0.5 + r2 * (A * r + B);
+                    dr = 3.0 * A * r + 2.0 * B;
+                } else {
+                    v = t * t * t;
+                    dr = -3.0 * t * t * ih / r;
+                }
                 const double w = double(q.z) + double(q.w);
                 sv += w * v;
                 sgx += w * dr * dx;
@@ -820,7 +853,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
     constexpr bool kScat = eval_scat(MODE);
     constexpr int kScatQ = kScat ? kEvalThreads * QPT : 1;   // an item's queries (make_items' chunk)
     __shared__ float4 s_sq[kScatQ];
-    __shared__ uint8_t s_sqf[kScatQ];
+    __shared__ uint16_t s_sqm[kScatQ];
 
     constexpr bool kF64 = MODE == EVAL_SPMV64;
     constexpr bool kComp = MODE == EVAL_SPMV32;
@@ -1022,7 +1055,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
                 const double w = a.qweight[r.id] * sig2;
                 const float wh = float(w);
                 s_sq[k] = make_float4(r.x, r.y, wh, float(w - double(wh)));
-                s_sqf[k] = uint8_t(r.flags & 63u);
+                s_sqm[k] = uint16_t(image_mask9(r.flags));
             }
             if (tid == 0 && it.qcnt > uint32_t(kScatQ)) atomicOr(a.flags, FLAG_CAPACITY);
         }
@@ -1129,7 +1162,7 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
 
             const int nbp = s_nbp;
             if constexpr (kScat)
-                scat_batch<ST, kScat9>(s_cand, s_bp, s_pc, nbp, s_btot, s_sq, s_sqf,
+                scat_batch<ST, kScat9>(s_cand, s_bp, s_pc, nbp, s_btot, s_sq, s_sqm,
                                        min(int(it.qcnt), kScatQ), G, a.out_f64);
             if constexpr (kPacked) {
                 // staged candidates -> image-shifted, bin-local coordinates + kappa c2
@@ -1304,6 +1337,16 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
 #pragma unroll
                         for (int j = 0; j < QPT; ++j) {
                             const GT dx = px[j] - cxd, dy = py[j] - cyd;   // q - c
+                            if constexpr (kGrad32) {
+                                // FP32 pairs without a branch (zeros outside the support)
+                                float v, dr;
+                                spline_vdr_f32(fmaf(dx, dx, dy * dy), hw, ih, A, B, v, dr);
+                                const float wdr = wd * dr;
+                                pv[j] = fmaf(wd, v, pv[j]);
+                                pgx[j] = fmaf(wdr, dx, pgx[j]);
+                                pgy[j] = fmaf(wdr, dy, pgy[j]);
+                                continue;
+                            }
                             const GT r2 = dx * dx + dy * dy;
                             const GT r = sqrt(r2);
                             if (r >= hw) continue;
