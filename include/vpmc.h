@@ -389,12 +389,12 @@ int vpmc_sim_vorticity_grid(vpmc_sim* sim, int inst, int res_x, int res_y, int s
  *     segment from its checkpoint and run the adjoint steps backwards; writes
  *     dL/dX_0 (2N doubles) and dL/domega (N doubles); the simulation is left
  *     in the recorded final state.  The trajectory is the forward's (its
- *     precision); the adjoint's field values and gradients at the samples
- *     and its transposed sums take their pairs in the forward's precision
- *     (for the FP32 path: FP32 pairs, summed into FP64 per candidate run,
- *     and the transposed sums compensated in FP32 per work item, then
- *     added in FP64); every MIS-term derivative and every accumulation
- *     across runs and items is FP64.
+ *     precision); the adjoint's field values and gradients at the samples,
+ *     its transposed sums and its MIS-term derivatives take their terms in
+ *     the forward's precision (for the FP32 path: FP32 pairs summed into
+ *     FP64 per candidate run, the transposed sums compensated in FP32 per
+ *     work item, FP32 MIS-term derivatives); every accumulation across
+ *     runs, items and samples is FP64.
  *     flags: VPMC_ADJ_SCORE adds the score-function term of the discrete
  *     branch-1 draw (P(I = J) = |omega_J| / Omega), which makes dL/domega an
  *     unbiased estimate of the gradient of the expected trajectory; without

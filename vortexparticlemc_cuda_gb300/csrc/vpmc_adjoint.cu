@@ -1,9 +1,10 @@
 // vpmc_adjoint.cu -- the adjoint of the plain MIS step (no counterpart in
 // the reference): checkpointed forward record, segment recompute, and per
-// step the value/gradient field sums at the samples (pairs in the forward's
-// precision), the per-sample FP64 derivatives of the MIS term, and the
-// transposed field sum at the particles.
+// step the value/gradient field sums at the samples, the per-sample
+// derivatives of the MIS term and the transposed field sum at the particles,
+// each term in the forward's precision and every sum in FP64.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "vpmc_sim.cuh"
@@ -27,48 +28,54 @@ using namespace sim;
 //              (the transposed field sum, evaluated with queries and candidates swapped)
 //   dL/domega_J through Omega: sgn(omega_J) (9 if periodic) sum_s dc_s/dOmega.
 
-// d(v . T)/d{x, f, Omega} of one MIS term in FP64 (mis_term64's arithmetic).
-__device__ __forceinline__ void mis_term_adj(int law, float2 xf, float2 yf, double f, double w1, double w2,
-                                             double cum, double alpha, double R, const InstMC& I, double vx,
-                                             double vy, double& gxx, double& gxy, double& df, double& dc,
-                                             double& cval) {
-    gxx = gxy = df = dc = cval = 0.0;
-    if (!(f > 0.0)) return;
-    const double rx = double(xf.x) - double(yf.x), ry = double(xf.y) - double(yf.y);
-    const double P = vy * rx - vx * ry;   // v . perp(r)
+// d(v . T)/d{x, f, Omega} of one MIS term (mis_term64's arithmetic), in R
+// arithmetic: FP64 on the FP64 path, FP32 on the FP32 path (each term is then
+// as precise as the forward's FP32 term; the caller accumulates in FP64).
+// The factor 1 - (w1 f / cum) / D of df/f is written as the disk term's share
+// w2 p2 / D, which equals it and has no cancellation when branch 1 dominates.
+template <typename R_>
+__device__ __forceinline__ void mis_term_adj(int law, float2 xf, float2 yf, R_ f, R_ w1, R_ w2, R_ cum, R_ alpha,
+                                             R_ R, const InstMC& I, R_ vx, R_ vy, R_& gxx, R_& gxy, R_& df, R_& dc,
+                                             R_& cval) {
+    gxx = gxy = df = dc = cval = R_(0);
+    if (!(f > R_(0))) return;
+    const R_ rx = R_(xf.x) - R_(yf.x), ry = R_(xf.y) - R_(yf.y);
+    const R_ P = vy * rx - vx * ry;   // v . perp(r)
+    const R_ two_pi = R_(2.0 * kPiD);
     if (law == VPMC_LAW_REFERENCE) {
-        double wx = rx, wy = ry;
+        R_ wx = rx, wy = ry;
         if (I.periodic) {
-            wx = rx - round(rx / I.Lx) * I.Lx;
-            wy = ry - round(ry / I.Ly) * I.Ly;
+            wx = rx - round(rx / R_(I.Lx)) * R_(I.Lx);
+            wy = ry - round(ry / R_(I.Ly)) * R_(I.Ly);
         }
-        const double wn = sqrt(wx * wx + wy * wy);
-        const double rn = fmax(wn, 1e-6);
-        const double inv = 1.0 / (rx * rx + ry * ry + 1e-8);
-        const double K = inv / (2.0 * kPiD);
-        const double denom = w1 * f / cum + w2 * alpha / rn;
-        const double sc = f / denom;
-        const double drx = wn > 1e-6 ? wx / wn : 0.0, dry = wn > 1e-6 ? wy / wn : 0.0;   // d rn / d r
-        const double g = sc / denom * (w2 * alpha / (rn * rn));                          // d sc / d rn
+        const R_ wn = sqrt(wx * wx + wy * wy);
+        const R_ rn = fmax(wn, R_(1e-6));
+        const R_ inv = R_(1) / (rx * rx + ry * ry + R_(1e-8));
+        const R_ K = inv / two_pi;
+        const R_ b2 = w2 * alpha / rn;   // the disk term of the denominator
+        const R_ denom = w1 * f / cum + b2;
+        const R_ sc = f / denom;
+        const R_ drx = wn > R_(1e-6) ? wx / wn : R_(0), dry = wn > R_(1e-6) ? wy / wn : R_(0);   // d rn / d r
+        const R_ g = sc / denom * (b2 / rn);                                                       // d sc / d rn
         cval = sc * K * P;
-        gxx = sc * K * vy - 2.0 * rx * inv * K * sc * P + K * P * g * drx;
-        gxy = -sc * K * vx - 2.0 * ry * inv * K * sc * P + K * P * g * dry;
-        df = K * P * (1.0 - f * w1 / (cum * denom)) / denom;
+        gxx = sc * K * vy - R_(2) * rx * inv * K * sc * P + K * P * g * drx;
+        gxy = -sc * K * vx - R_(2) * ry * inv * K * sc * P + K * P * g * dry;
+        df = K * P * (b2 / denom) / denom;
         dc = K * P * sc * (w1 * f / (cum * cum * denom));
         return;
     }
-    const double r2 = rx * rx + ry * ry;
-    if (!(r2 > 0.0)) return;
-    const double rn = sqrt(r2);
+    const R_ r2 = rx * rx + ry * ry;
+    if (!(r2 > R_(0))) return;
+    const R_ rn = sqrt(r2);
     const bool in = rn < R;
-    const double p2 = in ? alpha / rn : 0.0;
-    const double D = w1 * f / cum + w2 * p2;
-    const double sc = f / (D * 2.0 * kPiD * r2);
-    const double ex = (in ? -w2 * alpha / (rn * r2) : 0.0) / D + 2.0 / r2;   // -(d sc / d r) / (sc r)
+    const R_ p2 = in ? alpha / rn : R_(0);
+    const R_ D = w1 * f / cum + w2 * p2;
+    const R_ sc = f / (D * two_pi * r2);
+    const R_ ex = (in ? -w2 * alpha / (rn * r2) : R_(0)) / D + R_(2) / r2;   // -(d sc / d r) / (sc r)
     cval = sc * P;
     gxx = sc * vy - P * sc * ex * rx;
     gxy = -sc * vx - P * sc * ex * ry;
-    df = P * (1.0 - f * w1 / (cum * D)) / (2.0 * kPiD * r2 * D);
+    df = P * (w2 * p2 / D) / (two_pi * r2 * D);
     dc = P * sc * (w1 * f / (cum * cum * D));
 }
 
@@ -96,8 +103,11 @@ struct AdjArgs {
     double* csum;           // 2 per instance: sum of c over branch-1 samples
 };
 
-// One warp per target: the MIS-term derivatives of all its samples.
+// One warp per target: the MIS-term derivatives of all its samples, each in
+// FP32 (F32: the FP32 path) or FP64, every sum and atomic in FP64.
+template <bool F32>
 __global__ void __launch_bounds__(256) k_adj_terms(AdjArgs a) {
+    using R_ = typename std::conditional<F32, float, double>::type;
     const int lane = threadIdx.x & 31;
     const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const long nwarps = (long(gridDim.x) * blockDim.x) >> 5;
@@ -120,12 +130,14 @@ __global__ void __launch_bounds__(256) k_adj_terms(AdjArgs a) {
             double dca = 0.0, csa = 0.0;
             for (int j = lane; j < Q; j += 32) {
                 const long sid = base + j;
-                const double f = a.fg[3 * sid];
-                double gxx, gxy, df, dc, cv;
-                mis_term_adj(I.law, x, a.ys[sid], f, w1, w2, cum, alpha, R, I, vx, vy, gxx, gxy, df, dc, cv);
+                R_ gxr, gyr, dfr, dcr, cvr;
+                mis_term_adj<R_>(I.law, x, a.ys[sid], R_(a.fg[3 * sid]), R_(w1), R_(w2), R_(cum), R_(alpha), R_(R), I,
+                                 R_(vx), R_(vy), gxr, gyr, dfr, dcr, cvr);
+                const double gxx = gxr, gxy = gyr, df = dfr, dc = dcr, cv = cvr;
                 ltx += gxx;
                 lty += gxy;
-                const double dyx = -gxx + df * a.fg[3 * sid + 1], dyy = -gxy + df * a.fg[3 * sid + 2];
+                const double dyx = -gxx + double(dfr * R_(a.fg[3 * sid + 1]));
+                const double dyy = -gxy + double(dfr * R_(a.fg[3 * sid + 2]));
                 if (j >= a.N1) {
                     ltx += dyx;
                     lty += dyy;
@@ -270,7 +282,8 @@ int adjoint_step(vpmc_sim* s, AdjBufs& A, const double* lam_in, double* lam_out,
         VPMC_TRY(launch_eval(ctx, s->g, s->q.qrec, s->it, L));
         AdjArgs aa{s->d_mc, s->n_inst, s->pos, s->ys, A.fg, A.src, s->cum64, t0, nt, s->N1, s->N2, lam_in, lam_out,
                    A.as, A.dcum, score ? A.gsc : nullptr, A.csum};
-        VPMC_LAUNCH(k_adj_terms, blocks_for(nt * 32), 256, 0, st, aa);
+        if (f32) VPMC_LAUNCH(k_adj_terms<true>, blocks_for(nt * 32), 256, 0, st, aa);
+        else VPMC_LAUNCH(k_adj_terms<false>, blocks_for(nt * 32), 256, 0, st, aa);
         // transposed sums from the sample side: the same items, each sample
         // weighted by its dc/df, every in-support (sample, particle) pair adding
         // a_s W and a_s dW/dx_p to the particle's slot
