@@ -437,12 +437,16 @@ int vpmc_sim_set_precision(vpmc_sim* sim, int bits);
 
 /* Neighbour-walk tuning: cells per h_w (1 <= k <= 8; the walk covers the
  * (2k+1)^2 cells around a bin minus the corner cells beyond reach) and
- * queries per thread in the field-evaluation kernel (4, 6 or 8).  0 = auto. */
+ * queries per thread in the field-evaluation kernel (4, 6 or 8), or 1 for the
+ * tensor-core evaluation (squared distances of 128 queries x 128 candidates
+ * per tcgen05 multiply; plain kernels only, deformed kernels keep 4).
+ * 0 = default (k = 2, 4 queries per thread). */
 int vpmc_sim_set_tuning(vpmc_sim* sim, int k_walk, int queries_per_thread);
 int vpmc_sim_get_tuning(vpmc_sim* sim, int* k_walk, int* queries_per_thread);
 
 /* Autotuner (no reference counterpart): times one full MIS velocity pass per
- * candidate (k_walk, queries_per_thread) in {2..8}x{4} + {3,4,6,8}x{6} + {2,3,4,6,8}x{8}, keeps
+ * candidate (k_walk, queries_per_thread) in {2..8}x{4} + {3,4,6,8}x{6} + {2,3,4,6,8}x{8}
+ * + {3..8}x{1} (the tensor-core evaluation; not with deformed kernels), keeps
  * the fastest, and caches the choice in-process by (hwr, samples per target,
  * particles per h_w^2).  Results do not depend on the choice beyond FP32
  * rounding of the field sums, and the autotuner checks that: each

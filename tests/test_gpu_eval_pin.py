@@ -12,7 +12,9 @@ back the field value of every sample of a set of targets:
   * reference law (FIELD mode, the field queryVorticityAbs gives,
     include/vorticity_query.cuh:15-79): the periodic field at the wrapped point;
 
-for every (k_walk, queries per thread) in {5, 6, 7, 8} x {4, 6, 8}, within 1e-5
+for every (k_walk, queries per thread) in {5, 6, 7, 8} x {4, 6, 8}, and the
+tensor-core evaluation (squared distances from a 3xTF32 tcgen05 product, tuning
+value 1) at every k_walk, within 1e-5
 of the field's scale and, for every value above 1% of that scale, within 1e-5
 relative.  The velocities of all tunings agree target by target, and the
 unbiased estimator's 64-seed mean at k_walk = 7 lies within 3 standard errors
@@ -29,7 +31,7 @@ from conftest import to_dev
 pytestmark = pytest.mark.gpu
 
 NX, HWR, N1, N2 = 512, 16.0, 64, 64
-TUNINGS = [(k, q) for k in (5, 6, 7, 8) for q in (4, 6, 8)]
+TUNINGS = [(k, q) for k in (5, 6, 7, 8) for q in (4, 6, 8, 1)]   # q = 1: the tensor-core evaluation
 N_TARGETS = 24          # 24 x 256 = 6144 sample values per law and tuning
 STEP = 3
 
@@ -114,11 +116,12 @@ def test_sample_field_values_every_tuning(tg512, law_name):
     sim.set_law(P.LAW_UNBIASED)
 
 
-def test_unbiased_mean_within_3se_at_benchmark_tuning(tg512, cuda):
+@pytest.mark.parametrize("qpt", [4, 1])
+def test_unbiased_mean_within_3se_at_benchmark_tuning(tg512, cuda, qpt):
     from vortexparticlemc_cuda_gb300 import phash as P
     sim, sp, pos, om = tg512
     sim.set_law(P.LAW_UNBIASED)
-    sim.set_tuning(7, 4)
+    sim.set_tuning(7, qpt)
     targets = np.random.default_rng(4).choice(len(pos), 512, replace=False)
     tsel = torch.from_numpy(targets).to(cuda)
     seeds = 64

@@ -105,7 +105,8 @@ def test_advection_is_fp64_wrapped_euler(cuda):
     assert (p1 >= 0).all() and (p1 < 1).all()
 
 
-def test_ensemble_member_equals_standalone_run(cuda):
+@pytest.mark.parametrize("qpt", [4, 1])
+def test_ensemble_member_equals_standalone_run(cuda, qpt):
     from vortexparticlemc_cuda_gb300 import phash as P
     rng = np.random.default_rng(3)
     sizes = [32, 48, 40]
@@ -118,6 +119,7 @@ def test_ensemble_member_equals_standalone_run(cuda):
         om_all.append(om)
     ens = P.Simulation(params, [len(p) for p in pos_all])
     ens.set_particles(to_dev(np.concatenate(pos_all), cuda), to_dev(np.concatenate(om_all), cuda))
+    ens.set_tuning(0, qpt)
     ens.prepare()
     ens.step(2)
     pe, _, ve = ens.particles()
@@ -125,6 +127,7 @@ def test_ensemble_member_equals_standalone_run(cuda):
     for k in range(len(sizes)):
         one = P.Simulation(params[k], [len(pos_all[k])])
         one.set_particles(to_dev(pos_all[k], cuda), to_dev(om_all[k], cuda))
+        one.set_tuning(0, qpt)
         one.prepare()
         one.step(2)
         p1, _, v1 = one.particles()
@@ -146,7 +149,7 @@ def test_step_host_roundtrip(cuda):
 def test_tuning_does_not_change_results_beyond_rounding(cuda):
     sim, pos, om, prm = _setup(cuda, law=1)
     base = sim.velocity(step=1).cpu().numpy()
-    for k, q in ((1, 4), (3, 8), (2, 8), (4, 4), (3, 6), (2, 6)):
+    for k, q in ((1, 4), (3, 8), (2, 8), (4, 4), (3, 6), (2, 6), (1, 1), (2, 1), (4, 1)):
         sim.set_tuning(k, q)
         v = sim.velocity(step=1).cpu().numpy()
         assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max(), (k, q)
@@ -156,7 +159,7 @@ def test_autotune_picks_a_candidate_and_caches(cuda):
     sim, pos, om, prm = _setup(cuda, law=1)
     base = sim.velocity(step=2).cpu().numpy()
     k, q, ms = sim.autotune()
-    assert 2 <= k <= 8 and q in (4, 6, 8) and ms > 0
+    assert 2 <= k <= 8 and q in (1, 4, 6, 8) and ms > 0
     assert sim.tuning() == (k, q)
     v = sim.velocity(step=2).cpu().numpy()
     assert np.abs(v - base).max() <= 1e-4 * np.abs(base).max()

@@ -15,8 +15,8 @@ from conftest import to_dev
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("world,law", [(2, 1), (3, 0)])
-def test_sharded_run_equals_unsharded_bitwise(cuda, world, law):
+@pytest.mark.parametrize("world,law,qpt", [(2, 1, 4), (3, 0, 4), (2, 1, 1), (3, 0, 1)])
+def test_sharded_run_equals_unsharded_bitwise(cuda, world, law, qpt):
     from vortexparticlemc_cuda_gb300 import phash as P
     from vortexparticlemc_cuda_gb300.shard import ShardedSimulation
     Nx, steps = 96, 4
@@ -26,6 +26,7 @@ def test_sharded_run_equals_unsharded_bitwise(cuda, world, law):
     sp = P.SimParam(dt=1e-3, Nx=Nx, hwr=8, N1=16, N2=16, law=law, seed=5)
     whole = P.Simulation(sp, [len(pos)])
     whole.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+    whole.set_tuning(0, qpt)
     whole.prepare()
     whole.step(steps)
     want_pos, _, want_vel = (t.cpu().numpy() for t in whole.particles())
@@ -37,6 +38,7 @@ def test_sharded_run_equals_unsharded_bitwise(cuda, world, law):
     shards = [ShardedSimulation(sp, [len(pos)], r, world, allgather=gather_local) for r in range(world)]
     for s in shards:
         s.sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+        s.sim.set_tuning(0, qpt)
         s.sim.prepare()
     for _ in range(steps):
         for s in shards:

@@ -48,3 +48,28 @@ def test_expired_wait_returns_timeout_and_context_recovers(cuda):
     assert np.abs(out.cpu().numpy() - want).max() <= 1e-5 * np.abs(want).max()
     assert L.vpmc_context_sync(ctx.h) == 0
     ctx.close()
+
+
+@pytest.mark.parametrize("qpt", [1])
+def test_expired_wait_in_tensor_core_evaluation(cuda, qpt):
+    """The same for the tensor-core evaluation (tuning value 1), whose CTAs also
+    hold tensor memory: on expiry each CTA lets its copies and multiplies in
+    flight land and frees its tensor memory before it exits, so the next pass
+    on the same context runs normally and gives the same velocities."""
+    from vortexparticlemc_cuda_gb300 import phash as P
+    from vortexparticlemc_cuda_gb300._lib import WAIT_LIMIT_DEFAULT, VpmcError
+    pos = O.lattice(64)
+    om = O.taylor_green(pos)
+    sim = P.Simulation(P.SimParam(dt=1e-3, Nx=64, hwr=4, N1=16, N2=16, law=P.LAW_UNBIASED, seed=2), [len(pos)])
+    sim.set_particles(to_dev(pos, cuda), to_dev(om, cuda))
+    sim.set_tuning(3, qpt)
+    sim.prepare()
+    want = sim.velocity(step=1).cpu().numpy()
+    sim.ctx.set_wait_limit(0)
+    for _ in range(2):
+        with pytest.raises(VpmcError) as e:
+            sim.velocity(step=1)
+        assert e.value.status == 5               # VPMC_ERR_TIMEOUT
+    sim.ctx.set_wait_limit(WAIT_LIMIT_DEFAULT)
+    assert np.array_equal(sim.velocity(step=1).cpu().numpy(), want)
+    sim.close()

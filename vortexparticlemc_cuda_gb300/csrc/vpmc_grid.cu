@@ -607,39 +607,6 @@ struct EvalArgs {
     const double* qweight;    // SCAT modes: the weight of each query (by id)
 };
 
-// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction
-// serves two queries.  Operands are 64-bit register pairs {lo, hi}.
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x pk2(float a, float b) {
-    f2x r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void up2(f2x v, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2x add2(f2x a, f2x b) {
-    f2x r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
-    f2x r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
-    f2x r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-__device__ __forceinline__ float sqrt_approx(float x) {
-    float r;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 // Sum over one staged run of candidates for NPR packed query pairs, in
 // bin-local coordinates, every squared distance pre-scaled by kappa = -3/h^2:
 // candidates hold (x, y) relative to the bin centre and kappa c2; queries
@@ -652,7 +619,6 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 // Per pair of queries: 7 packed FMA-pipe operations + 2 saturating scalar FMAs,
 // 2 square roots on the XU and 2 min on the ALU.  The candidate loop is unrolled
 // four times (independent chains across candidates; still 64 registers).
-constexpr float kInvSqrt3 = 0.57735026918962576f;
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
                                            const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX]) {
@@ -1523,7 +1489,7 @@ int blocks_for(long n, int threads = 256) {
 
 int default_k() { return 2; }
 
-int query_chunk(int qpt) { return (qpt == 8 ? 8 : qpt == 6 ? 6 : 4) * kEvalThreads; }
+int query_chunk(int qpt) { return (qpt == 8 ? 8 : qpt == 6 ? 6 : 4) * kEvalThreads; }   // qpt 1 (tensor cores): 128
 
 long grid_plan(const InstDesc* in, int n, int k, int nsets, GridInst* out) {
     if (k <= 0) k = default_k();
@@ -1724,6 +1690,11 @@ int bin_points(vpmc_context* ctx, const GridBufs& g, QueryBufs& q, const float2*
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L) {
     if (eval_deformed(L.mode) && !g.candf) return VPMC_ERR_INVALID;
     if (eval_scat(L.mode) && (!L.qweight || !L.out_f64 || L.qpt != 4)) return VPMC_ERR_INVALID;
+    if (L.qpt == 1 && (L.mode == EVAL_FIELD || L.mode == EVAL_FIELD9)) {
+        const EvalTcArgs t{g.inst, g.start, L.rows > 0 ? L.rows : g.rows, g.cand, qrec, it.items, it.n_items,
+                           it.counter, L.out_f32, ctx->d_flags, ctx->wait_limit};
+        return launch_eval_tc(ctx, t, L.mode == EVAL_FIELD9);
+    }
     EvalArgs a{g.inst, g.start, L.rows > 0 ? L.rows : g.rows, g.cand, g.candf, qrec, it.items, it.n_items, it.counter,
                L.out_f32, L.out_f64, ctx->d_flags, ctx->wait_limit, L.qweight};
     switch (L.mode) {

@@ -68,6 +68,42 @@ struct Item {
     uint32_t inst;
 };
 
+// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction
+// serves two queries.  Operands are 64-bit register pairs {lo, hi}.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk2(float a, float b) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(f2x v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+    f2x r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// 1/sqrt(3): the packed spline works with sqrt(3) r/h (see packed_run).
+constexpr float kInvSqrt3 = 0.57735026918962576f;
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 enum EvalMode : int {
     EVAL_FIELD = 0,      // out_f32[id] = sum w W          (periodic / plain field)
     EVAL_FIELD9 = 1,     // as FIELD, only images m in {-1,0,1}^2 of the unwrapped point
@@ -214,11 +250,28 @@ int grid_max_sigma(vpmc_context* ctx, const float4* F, long n, unsigned* d_words
 struct EvalLaunch {
     int mode = EVAL_FIELD;
     int rows = -1;             // candidate sub-rows per cell of the candidate ranges (-1: the grid's)
-    int qpt = 4;               // queries per thread (FIELD modes: 4 or 8; others: 4)
+    int qpt = 4;               // queries per thread (FIELD modes: 4, 6 or 8, or 1 = the tensor-core evaluation; others: 4)
     float* out_f32 = nullptr;
     double* out_f64 = nullptr;
     const double* qweight = nullptr;   // SCAT modes: weight of each query, by query id
 };
 int launch_eval(vpmc_context* ctx, const GridBufs& g, const QRec* qrec, ItemBufs& it, const EvalLaunch& L);
+
+// The FIELD / FIELD9 evaluation with the squared distances on the tensor cores
+// (vpmc_eval_tc.cu; selected by EvalLaunch::qpt == 1, items of 128 queries).
+struct EvalTcArgs {
+    const GridInst* inst;
+    const uint32_t* cstart;   // candidate range per sub-row
+    int rows;                 // sub-rows per cell
+    const Cand* cand;
+    const QRec* qrec;
+    const Item* items;
+    const uint32_t* n_items;
+    uint32_t* counter;
+    float* out;               // out[id] = sum w W
+    unsigned* flags;
+    uint32_t wait_limit;
+};
+int launch_eval_tc(vpmc_context* ctx, const EvalTcArgs& a, bool field9);
 
 }  // namespace vpmc

@@ -1308,7 +1308,8 @@ int vpmc_sim_set_rbf_solver(vpmc_sim* s, int solver) {
 }
 
 int vpmc_sim_set_tuning(vpmc_sim* s, int k_walk, int qpt) {
-    if (!s || k_walk < 0 || k_walk > 8 || !(qpt == 0 || qpt == 4 || qpt == 6 || qpt == 8)) return VPMC_ERR_INVALID;
+    if (!s || k_walk < 0 || k_walk > 8 || !(qpt == 0 || qpt == 1 || qpt == 4 || qpt == 6 || qpt == 8))
+        return VPMC_ERR_INVALID;
     s->k_walk = k_walk;
     s->qpt = qpt == 0 ? 4 : qpt;
     VPMC_TRY(alloc_work(s));
@@ -1344,11 +1345,15 @@ int vpmc_sim_autotune(vpmc_sim* s, int* k_out, int* qpt_out, float* best_ms) {
         }
     }
     cudaStream_t st = s->ctx->stream;
+    // queries per thread 4, 6, 8: the one-warp CUDA-core evaluation; 1: the
+    // tensor-core evaluation (plain kernels only: deformed ones run the former)
     const int cands[][2] = {{2, 4}, {3, 4}, {4, 4}, {5, 4}, {6, 4}, {7, 4}, {8, 4}, {3, 6}, {4, 6}, {6, 6},
-                            {8, 6}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}};
+                            {8, 6}, {2, 8}, {3, 8}, {4, 8}, {6, 8}, {8, 8}, {3, 1}, {4, 1}, {5, 1}, {6, 1},
+                            {7, 1}, {8, 1}};
     struct Trial { int k, q; float ms; double check; };
     std::vector<Trial> tr;
     for (const auto& c : cands) {
+        if (c[1] == 1 && s->deform) continue;
         if (vpmc_sim_set_tuning(s, c[0], c[1]) != VPMC_OK) continue;
         if (s->plan[0].k != c[0]) continue;   // geometry clamped k: skip duplicates
         int nl = 0;
