@@ -564,6 +564,13 @@ def run_gpu(args, wl):
             "eval_ms_per_launch": eval_ms_launch, "eval_share_of_step": float(np.mean(eval_ms)) / (ms / args.steps)}
     if clocks.get("sm_mhz"):
         roof["frac_at_sampled_clock"] = achieved / (sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
+    # the whole step against the same peak: Q (n_hit 16 + 40) flop per
+    # particle-step (16 per in-support pair, ~40 of MIS arithmetic per sample)
+    step_flop = samples_launch * launches * (n_hit * 16.0 + 40.0)
+    step_achieved = step_flop / (ms / args.steps / 1e3) / 1e12
+    roof["step"] = {"achieved": step_achieved, "frac": step_achieved / fp32_peak, "unit": "TFLOP/s",
+                    "algorithmic": f"{samples_launch * launches:.0f} sample queries x ({n_hit:.1f} pairs x 16 + 40) "
+                                   "flop per step"}
 
     log(f"e2e {e2e['value']:.3e} particle-steps/s")
     cpu = None
