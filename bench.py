@@ -140,6 +140,12 @@ def job_throughput(units_per_job: int, steps: int, ms_max: float) -> float:
     return units_per_job * steps / (ms_max / 1e3)
 
 
+def step_flop_rate(sample_queries: float, n_hit: float, ms_per_step: float) -> float:
+    """TFLOP/s of a whole step by the algorithmic count: per sample query,
+    16 flop per in-support pair plus ~40 flop of MIS arithmetic."""
+    return sample_queries * (n_hit * 16.0 + 40.0) / (ms_per_step / 1e3) / 1e12
+
+
 def reports(rank: int) -> bool:
     """Only rank 0 prints the JSON line (and runs the CPU reference arm)."""
     return rank == 0
@@ -566,8 +572,7 @@ def run_gpu(args, wl):
         roof["frac_at_sampled_clock"] = achieved / (sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
     # the whole step against the same peak: Q (n_hit 16 + 40) flop per
     # particle-step (16 per in-support pair, ~40 of MIS arithmetic per sample)
-    step_flop = samples_launch * launches * (n_hit * 16.0 + 40.0)
-    step_achieved = step_flop / (ms / args.steps / 1e3) / 1e12
+    step_achieved = step_flop_rate(samples_launch * launches, n_hit, ms / args.steps)
     roof["step"] = {"achieved": step_achieved, "frac": step_achieved / fp32_peak, "unit": "TFLOP/s",
                     "algorithmic": f"{samples_launch * launches:.0f} sample queries x ({n_hit:.1f} pairs x 16 + 40) "
                                    "flop per step"}

@@ -85,3 +85,14 @@ def test_samples_the_unbiased_law_drops_count_zero():
     assert bench.in_support_pairs(_Stand(pos, om, far), [_param()], [len(pos)], n_targets=4) == 0.0
     # the reference law keeps them (wrapped)
     assert bench.in_support_pairs(_Stand(pos, om, far), [_param(LAW_REFERENCE)], [len(pos)], n_targets=4) > 0.0
+
+
+def test_step_flop_rate_is_the_surveys_count():
+    """Whole-step roofline: Q (n_hit 16 + 40) flop per particle-step over the
+    step time -- the tg2048 line (2^30 sample queries, 600.6 pairs, 308.8 ms)
+    is 33.6 TFLOP/s."""
+    import bench
+    r = bench.step_flop_rate(2 ** 30, 600.6, 308.8)
+    assert abs(r - 2 ** 30 * (600.6 * 16 + 40) / 0.3088 / 1e12) < 1e-9
+    assert 33.5 < r < 33.7
+    assert bench.step_flop_rate(1e6, 0.0, 1.0) == 1e6 * 40.0 / 1e-3 / 1e12
