@@ -502,13 +502,20 @@ __global__ void __launch_bounds__(kAsmThreads, 2) k_scatter_assemble(const uint4
                 r[j] = make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), q.id, q.flags);
             }
             __syncthreads();
-            for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-                uint32_t off = cnt[b];
+            // each bin's 16 sub-cell counters -> first slots, by warp 0: two bins
+            // per pass, one counter per lane, a scan inside each 16-lane half
+            if (threadIdx.x < 32) {
+                const uint32_t lane = threadIdx.x, c = lane & 15u;
+                for (uint32_t b = lane >> 4; b < ((nb + 1u) & ~1u); b += 2u) {
+                    const bool live = b < nb;
+                    const uint32_t n = live ? sub[c * nb + b] : 0u;
+                    uint32_t incl = n;
 #pragma unroll
-                for (int c = 0; c < kSubCells; ++c) {
-                    const uint32_t n = sub[uint32_t(c) * nb + b];
-                    sub[uint32_t(c) * nb + b] = off;
-                    off += n;
+                    for (int o = 1; o < 16; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 16);
+                        if (c >= uint32_t(o)) incl += y;
+                    }
+                    if (live) sub[c * nb + b] = cnt[b] + incl - n;
                 }
             }
             __syncthreads();
