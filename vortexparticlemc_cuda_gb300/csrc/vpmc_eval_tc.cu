@@ -319,39 +319,11 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_eval_tc(EvalTcArgs
             }
             const int R = a.rows, gyR = G.gy * R;
             const uint32_t colbase = (uint32_t(G.bin_base) + set * ncell) * uint32_t(R);
-            const float sx = 1.f / G.inv_sx, reach2 = G.reach * G.reach;
+            const float sx = 1.f / G.inv_sx;
             const float srow = 1.f / (G.inv_sy * float(R)), inv_srow = G.inv_sy * float(R);
             const float rm = G.reach * 1.001f;
-            const int ox = lane - G.k;
-            int gxx = cx + ox, sxi = 0;
-            int r0[2] = {1, 1}, r1[2] = {0, 0}, syi[2] = {0, 0};
-            const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
-            bool col = ox <= G.k && dx * dx <= reach2;
-            if (col) {
-                if (G.periodic) {
-                    if (gxx < 0) { gxx += G.gx; sxi = -1; }
-                    else if (gxx >= G.gx) { gxx -= G.gx; sxi = 1; }
-                } else if (gxx < 0 || gxx >= G.gx) {
-                    col = false;
-                }
-            }
-            if (col) {
-                const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * inv_srow - 1e-3f)), G.k * R);
-                const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
-                if (G.periodic) {
-                    if (ylo < 0) {
-                        r0[0] = 0; r1[0] = yhi;
-                        r0[1] = ylo + gyR; r1[1] = gyR - 1; syi[1] = -1;
-                    } else if (yhi >= gyR) {
-                        r0[0] = ylo; r1[0] = gyR - 1;
-                        r0[1] = 0; r1[1] = yhi - gyR; syi[1] = 1;
-                    } else {
-                        r0[0] = ylo; r1[0] = yhi;
-                    }
-                } else {
-                    r0[0] = max(ylo, 0); r1[0] = min(yhi, gyR - 1);
-                }
-            }
+            int gxx, sxi, r0[2], r1[2], syi[2];
+            walk_column(G, cx, cy, R, lane, gxx, sxi, r0, r1, syi);
             uint32_t gs[2] = {0u, 0u}, cn[2] = {0u, 0u};
             int img[2] = {0, 0};
             float fox[2] = {0.f, 0.f}, foy[2] = {0.f, 0.f};

@@ -886,42 +886,8 @@ __global__ void __launch_bounds__(kEvalThreads, eval_min_blocks(MODE, QPT)) k_ev
             const int cx = int(cell) / G.gy, cy = int(cell) % G.gy;
             const int R = a.rows, gyR = G.gy * R;
             const uint32_t colbase = (uint32_t(G.bin_base) + set * ncell) * uint32_t(R);
-            const float sx = 1.f / G.inv_sx, reach2 = G.reach * G.reach;
-            const int ox = lane - G.k;
-            int gxx = cx + ox, sxi = 0;
-            int r0[2] = {1, 1}, r1[2] = {0, 0}, syi[2] = {0, 0};   // empty unless set below
-            // the column is at least dx from every point of the bin's cell; its
-            // candidates within reach lie within dy = sqrt(reach^2 - dx^2) of the
-            // cell in y: sub-rows [cy R - m, cy R + R - 1 + m]
-            const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
-            bool col = ox <= G.k && dx * dx <= reach2;
-            if (col) {
-                if (G.periodic) {
-                    if (gxx < 0) { gxx += G.gx; sxi = -1; }
-                    else if (gxx >= G.gx) { gxx -= G.gx; sxi = 1; }
-                } else if (gxx < 0 || gxx >= G.gx) {
-                    col = false;
-                }
-            }
-            if (col) {
-                // (1e-3 of a sub-row of tolerance: the pairs it can skip lie within 0.2% of
-                // the kernel's support edge, where W / W(0) < 1e-7)
-                const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * G.inv_sy * float(R) - 1e-3f)), G.k * R);
-                const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
-                if (G.periodic) {
-                    if (ylo < 0) {
-                        r0[0] = 0; r1[0] = yhi;
-                        r0[1] = ylo + gyR; r1[1] = gyR - 1; syi[1] = -1;
-                    } else if (yhi >= gyR) {
-                        r0[0] = ylo; r1[0] = gyR - 1;
-                        r0[1] = 0; r1[1] = yhi - gyR; syi[1] = 1;
-                    } else {
-                        r0[0] = ylo; r1[0] = yhi;
-                    }
-                } else {
-                    r0[0] = max(ylo, 0); r1[0] = min(yhi, gyR - 1);
-                }
-            }
+            int gxx, sxi, r0[2], r1[2], syi[2];
+            walk_column(G, cx, cy, R, lane, gxx, sxi, r0, r1, syi);
             uint32_t rs[2] = {0u, 0u}, re[2] = {0u, 0u};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {

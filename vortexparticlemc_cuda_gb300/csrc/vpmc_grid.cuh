@@ -104,6 +104,53 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return r;
 }
 
+// One column of a bin's walk (lane = 0 .. 2k of a warp; column ox = lane - k
+// cells from the bin's cell (cx, cy) in x): the grid column gxx it reads, the
+// periodic image sxi it lies in, and its sub-rows [r0[h], r1[h]] in up to two
+// runs (a periodic column wrapping in y splits; image syi[h]).  The column is
+// at least dx from every point of the bin's cell, so its candidates within
+// reach lie within dy = sqrt(reach^2 - dx^2) of the cell in y: sub-rows
+// [cy R - m, cy R + R - 1 + m] (1e-3 of a sub-row of tolerance: the pairs it
+// can skip lie within 0.2% of the kernel's support edge, where W / W(0) <
+// 1e-7).  Runs left empty have r0 > r1.
+__device__ __forceinline__ void walk_column(const GridInst& G, int cx, int cy, int R, int lane, int& gxx, int& sxi,
+                                            int (&r0)[2], int (&r1)[2], int (&syi)[2]) {
+    const int gyR = G.gy * R;
+    const float sx = 1.f / G.inv_sx, reach2 = G.reach * G.reach;
+    const int ox = lane - G.k;
+    gxx = cx + ox;
+    sxi = 0;
+    r0[0] = r0[1] = 1;
+    r1[0] = r1[1] = 0;
+    syi[0] = syi[1] = 0;
+    const float dx = ox == 0 ? 0.f : float(abs(ox) - 1) * sx;
+    bool col = ox <= G.k && dx * dx <= reach2;
+    if (col) {
+        if (G.periodic) {
+            if (gxx < 0) { gxx += G.gx; sxi = -1; }
+            else if (gxx >= G.gx) { gxx -= G.gx; sxi = 1; }
+        } else if (gxx < 0 || gxx >= G.gx) {
+            col = false;
+        }
+    }
+    if (!col) return;
+    const int m = min(int(ceilf(sqrtf(reach2 - dx * dx) * G.inv_sy * float(R) - 1e-3f)), G.k * R);
+    const int ylo = cy * R - m, yhi = cy * R + R - 1 + m;
+    if (G.periodic) {
+        if (ylo < 0) {
+            r0[0] = 0; r1[0] = yhi;
+            r0[1] = ylo + gyR; r1[1] = gyR - 1; syi[1] = -1;
+        } else if (yhi >= gyR) {
+            r0[0] = ylo; r1[0] = gyR - 1;
+            r0[1] = 0; r1[1] = yhi - gyR; syi[1] = 1;
+        } else {
+            r0[0] = ylo; r1[0] = yhi;
+        }
+    } else {
+        r0[0] = max(ylo, 0); r1[0] = min(yhi, gyR - 1);
+    }
+}
+
 enum EvalMode : int {
     EVAL_FIELD = 0,      // out_f32[id] = sum w W          (periodic / plain field)
     EVAL_FIELD9 = 1,     // as FIELD, only images m in {-1,0,1}^2 of the unwrapped point
