@@ -433,6 +433,9 @@ class Simulation:
         check(lib().vpmc_sim_set_precision(self.h, int(bits)), "vpmc_sim_set_precision")
 
     def set_tuning(self, k_walk: int = 0, queries_per_thread: int = 0):
+        """Cells per h_w of the evaluation walk (1..8) and the evaluation kernel:
+        queries_per_thread 4, 6 or 8 for the one-warp CUDA-core kernel, 1 for the
+        tensor-core kernel (plain kernels; deformed ones keep 4).  0 = default."""
         check(lib().vpmc_sim_set_tuning(self.h, int(k_walk), int(queries_per_thread)), "vpmc_sim_set_tuning")
 
     def autotune(self):
