@@ -625,12 +625,14 @@ struct EvalArgs {
 // and beyond the support t = 0 leaves min(1/2, 0) = 0.
 // Per pair of queries: 7 packed FMA-pipe operations + 2 saturating scalar FMAs,
 // 2 square roots on the XU and 2 min on the ALU.  The candidate loop is unrolled
-// four times (independent chains across candidates; still 64 registers).
+// eight times (independent chains across candidates, 80 registers; at tg2048
+// 257.7 ms per evaluation against 261.1 unrolled four times, 274.4 twice,
+// 272.5 twelve times, 258.4 sixteen times).
 template <int NPR, int NPMAX>
 __device__ __forceinline__ void packed_run(const Cand* __restrict__ cs, int cnt, const f2x (&QX)[NPMAX],
                                            const f2x (&QY)[NPMAX], const f2x (&Q2)[NPMAX], f2x (&P)[NPMAX]) {
     const f2x HALF = pk2(0.5f, 0.5f);
-#pragma unroll 4
+#pragma unroll 8
     for (int c = 0; c < cnt; ++c) {
         const ulonglong2 XY = *reinterpret_cast<const ulonglong2*>(&cs[c].x);
         const ulonglong2 WC = *reinterpret_cast<const ulonglong2*>(&cs[c].w);   // (w, w), (kappa c2, kappa c2)
