@@ -317,12 +317,14 @@ __device__ __forceinline__ float2 mis_term(int law, float2 x, float2 y, float f,
     const float r2 = rx * rx + ry * ry;
     if (!(r2 > 0.f)) return make_float2(0.f, 0.f);
     // K(x - y) f / (w1 f / cum + w2 p2(|x - y|)), p2 = alpha / r inside the disk:
-    // multiplied through by cum r, one division per term
+    // multiplied through by cum r, one division per term (the fast form, a
+    // reciprocal and a product: ~2 ulp, far below the estimator's noise)
     //   sc = f cum r / ((w1 f r + w2 alpha cum) 2 pi r^2)   (inside)
     //   sc = cum / (w1 2 pi r^2)                             (outside)
     const float rn = sqrtf(r2);
     const float tpr2 = 2.f * kPiF * r2;
-    const float sc = rn < R ? (f * cum * rn) / (fmaf(w1 * f, rn, w2 * alpha * cum) * tpr2) : cum / (w1 * tpr2);
+    const float sc = rn < R ? __fdividef(f * cum * rn, fmaf(w1 * f, rn, w2 * alpha * cum) * tpr2)
+                            : __fdividef(cum, w1 * tpr2);
     return make_float2(-ry * sc, rx * sc);
 }
 

@@ -99,7 +99,7 @@ struct vpmc_sim {
     int N1 = 0, N2 = 0;
     uint64_t step = 0;
     int k_walk = 0, qpt = 4;
-    int rows = 16;                     // candidate sub-rows per cell of the evaluation grid
+    int rows = 32;                     // candidate sub-rows per cell of the evaluation grid
     bool prepared = false;
     // device state
     DevBuf mem;                        // particles, subsets, tables
