@@ -14,7 +14,7 @@ namespace {
 constexpr int kEvalThreads = 32;
 constexpr int kMaxK = 8;
 constexpr int kMaxPieces = 2 * (2 * kMaxK + 1);
-constexpr int kCandCap = 200;                  // candidates staged per batch (6.25 KB: 24 one-warp CTAs per SM)
+constexpr int kCandCap = 208;                  // candidates staged per batch (6.5 KB: 24 one-warp CTAs fill an SM's shared memory)
 constexpr uint32_t kWaitLimit = VPMC_WAIT_LIMIT_DEFAULT;   // drain wait of an aborted CTA (always the full cap)
 
 __device__ __forceinline__ int inst_of_particle(const GridInst* inst, int n_inst, long i) {
@@ -805,7 +805,7 @@ __device__ __forceinline__ void scat_batch(const Cand* __restrict__ s_cand, cons
     }
 }
 
-// The packed FP32 kernels run one-warp CTAs, 24 per SM (their 6.25 KB staging
+// The packed FP32 kernels run one-warp CTAs, 24 per SM (their 6.5 KB staging
 // buffers fit 24 times in shared memory; 85 registers a thread at most) with 4
 // queries per thread, 16 per SM with 6 and 12 with 8.  One warp per CTA: no warp of an item
 // waits at a barrier for another.
